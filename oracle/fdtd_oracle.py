@@ -1,0 +1,370 @@
+"""NumPy restatement of the reference fdtd2d engine: TEST INFRASTRUCTURE ONLY.
+
+This module is the oracle that the tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` use to check the CUDA engine in
+``soundwavesimulation_gb300``. The product never imports, links or runs it.
+
+Every function restates one piece of the reference (scjoshi/SoundWaveSimulation)
+and cites the file:line it follows. Arithmetic runs in the dtype of the inputs
+(float64 by default), vectorised over a leading shot axis where the reference
+batches shots. Parity of this restatement with the reference itself is pinned by
+``tests/golden/*.npz`` (produced by running the reference, see
+``tests/golden/make_golden.py``) and checked in ``tests/test_oracle_golden.py``.
+
+Array conventions follow the reference: fields are ``(shots, ny, nx)`` with
+row = y and column = x; traces are ``(shots, receivers, steps)``.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+
+# ---------------------------------------------------------------------------
+# Grid helpers (fdtd2d/experiment.py)
+# ---------------------------------------------------------------------------
+
+def axis_centers(n, spacing):
+    """Cell-centre axis, origin at the grid centre (fdtd2d/experiment.py:6-8)."""
+    return (np.arange(n) - 0.5 * (n - 1)) * spacing
+
+
+def stable_dt(c_max, dx, dy, cfl=0.45):
+    """CFL time step (fdtd2d/experiment.py:11-13)."""
+    return cfl / (c_max * np.sqrt(1.0 / dx**2 + 1.0 / dy**2))
+
+
+def n_steps_for_crossing(radius_m, c_min, dt, extras=1.6):
+    """Steps to cross the ring diameter with margin (fdtd2d/experiment.py:16-18)."""
+    return int(np.ceil(extras * (2.0 * radius_m / c_min) / dt))
+
+
+# ---------------------------------------------------------------------------
+# Ring geometry (fdtd2d/array.py)
+# ---------------------------------------------------------------------------
+
+def ring_geometry(n_elements, radius_m, x_m, y_m, center=(0.0, 0.0)):
+    """Element positions, nearest nodes and bilinear taps of a ring.
+
+    Restates RingArray.__init__ / _nearest_indices / _init_bilinear
+    (fdtd2d/array.py:14-33 and 60-76). Returns a dict of arrays.
+    """
+    theta = 2.0 * np.pi * np.arange(n_elements) / n_elements
+    x = center[0] + radius_m * np.cos(theta)
+    y = center[1] + radius_m * np.sin(theta)
+    return _geometry_from_points(x, y, np.asarray(x_m, float), np.asarray(y_m, float))
+
+
+def arc_geometry(n_elements, radius_m, span_deg, center_deg, x_m, y_m, center=(0.0, 0.0)):
+    """Elements equally spaced on an arc (ArcArray.__init__, fdtd2d/array.py:126-150)."""
+    half = 0.5 * np.deg2rad(span_deg)
+    theta = np.deg2rad(center_deg) + np.linspace(-half, half, n_elements)
+    x = center[0] + radius_m * np.cos(theta)
+    y = center[1] + radius_m * np.sin(theta)
+    return _geometry_from_points(x, y, np.asarray(x_m, float), np.asarray(y_m, float))
+
+
+def _geometry_from_points(x, y, x_axis, y_axis):
+    dx = x_axis[1] - x_axis[0]
+    dy = y_axis[1] - y_axis[0]
+    cols = np.rint((x - x_axis[0]) / dx).astype(np.int64)  # array.py:28-33
+    rows = np.rint((y - y_axis[0]) / dy).astype(np.int64)
+    colf = (x - x_axis[0]) / dx  # array.py:60-76
+    rowf = (y - y_axis[0]) / dy
+    col0 = np.floor(colf).astype(np.int64)
+    row0 = np.floor(rowf).astype(np.int64)
+    wx = colf - col0
+    wy = rowf - row0
+    return {
+        "x": x, "y": y, "rows": rows, "cols": cols,
+        "row0": row0, "col0": col0, "row1": row0 + 1, "col1": col0 + 1,
+        "w00": (1.0 - wx) * (1.0 - wy), "w10": wx * (1.0 - wy),
+        "w01": (1.0 - wx) * wy, "w11": wx * wy,
+    }
+
+
+# ---------------------------------------------------------------------------
+# Source waveform (fdtd2d/torch_backend.py:80-102)
+# ---------------------------------------------------------------------------
+
+def linear_chirp(dt, duration_s, f_start_hz, f_end_hz):
+    """Hann-windowed linear chirp as the torch backend builds it.
+
+    Restates torch_backend.linear_chirp (fdtd2d/torch_backend.py:80-102): the
+    sweep rate uses ``(n_pulse - 1) * dt`` and the Hann window ``n_pulse - 1``.
+    """
+    n_pulse = max(int(round(duration_s / dt)), 2)
+    t = np.arange(n_pulse) * dt
+    sweep = (f_end_hz - f_start_hz) / float((n_pulse - 1) * dt)
+    phase = 2.0 * np.pi * (f_start_hz * t + 0.5 * sweep * t * t)
+    window = 0.5 - 0.5 * np.cos(2.0 * np.pi * np.arange(n_pulse) / (n_pulse - 1))
+    return window * np.sin(phase)
+
+
+# ---------------------------------------------------------------------------
+# Stencil, Mur edges, one leapfrog step (fdtd2d/torch_backend.py)
+# ---------------------------------------------------------------------------
+
+def laplacian(u, dx, dy):
+    """5-point Laplacian with zero padding, evaluated at every node.
+
+    Restates the 3x3 conv2d kernel with ``padding=1`` (fdtd2d/torch_backend.py:
+    122-132 and 170-174). Works on ``(..., ny, nx)``.
+    """
+    inv_dx2 = 1.0 / dx**2
+    inv_dy2 = 1.0 / dy**2
+    p = np.zeros(u.shape[:-2] + (u.shape[-2] + 2, u.shape[-1] + 2), dtype=u.dtype)
+    p[..., 1:-1, 1:-1] = u
+    return (
+        (p[..., 1:-1, :-2] + p[..., 1:-1, 2:]) * inv_dx2
+        + (p[..., :-2, 1:-1] + p[..., 2:, 1:-1]) * inv_dy2
+        - 2.0 * (inv_dx2 + inv_dy2) * u
+    )
+
+
+def mur_coefficients(c, dt, dx, dy):
+    """First-order Mur coefficients (fdtd2d/torch_backend.py:264-275)."""
+    c = np.asarray(c)
+    k = {
+        "left": (c[1:-1, 0] * dt - dx) / (c[1:-1, 0] * dt + dx),
+        "right": (c[1:-1, -1] * dt - dx) / (c[1:-1, -1] * dt + dx),
+        "bottom": (c[0, 1:-1] * dt - dy) / (c[0, 1:-1] * dt + dy),
+        "top": (c[-1, 1:-1] * dt - dy) / (c[-1, 1:-1] * dt + dy),
+    }
+    corners = np.array([c[0, 0], c[0, -1], c[-1, 0], c[-1, -1]])
+    k["corner_kx"] = (corners * dt - dx) / (corners * dt + dx)
+    k["corner_ky"] = (corners * dt - dy) / (corners * dt + dy)
+    return k
+
+
+_CORNERS = ((0, 0, 1, 1), (0, -1, 1, -2), (-1, 0, -2, 1), (-1, -1, -2, -2))
+
+
+def apply_mur(u, u_next, k):
+    """Mur edges, then corners from the already updated edges, in place.
+
+    Restates _apply_mur_batch (fdtd2d/torch_backend.py:477-490), which is the
+    batched form of the single-shot update at 212-232 and of the NumPy
+    FDTD2D._apply_mur / _mur_corner (fdtd2d/solver.py:90-124). Works on
+    ``(..., ny, nx)``.
+    """
+    u_next[..., 1:-1, 0] = u[..., 1:-1, 1] + k["left"] * (u_next[..., 1:-1, 1] - u[..., 1:-1, 0])
+    u_next[..., 1:-1, -1] = u[..., 1:-1, -2] + k["right"] * (u_next[..., 1:-1, -2] - u[..., 1:-1, -1])
+    u_next[..., 0, 1:-1] = u[..., 1, 1:-1] + k["bottom"] * (u_next[..., 1, 1:-1] - u[..., 0, 1:-1])
+    u_next[..., -1, 1:-1] = u[..., -2, 1:-1] + k["top"] * (u_next[..., -2, 1:-1] - u[..., -1, 1:-1])
+    vals = []
+    for i, (r, c, ri, ci) in enumerate(_CORNERS):
+        cu = u[..., r, c]
+        from_x = u[..., r, ci] + k["corner_kx"][i] * (u_next[..., r, ci] - cu)
+        from_y = u[..., ri, c] + k["corner_ky"][i] * (u_next[..., ri, c] - cu)
+        vals.append(0.5 * (from_x + from_y))
+    for (r, c, _, _), v in zip(_CORNERS, vals):
+        u_next[..., r, c] = v
+    return u_next
+
+
+def forward_step(u_old, u, c2, dt2, dx, dy, k, source=None):
+    """One forward leapfrog step ``u+ = 2u - u- + dt^2 c^2 lap(u) + s``, then Mur.
+
+    Restates _advance_field / _advance_field_batch (fdtd2d/torch_backend.py:
+    177-233 and 493-522): the soft source is added to ``u+`` before the Mur
+    edges overwrite the boundary. ``source`` is None or an array broadcastable
+    to ``u`` (a dense field holding the nearest-node or bilinear injection).
+    """
+    u_next = 2.0 * u - u_old + dt2 * c2 * laplacian(u, dx, dy)
+    if source is not None:
+        u_next = u_next + source
+    return apply_mur(u, u_next, k)
+
+
+def adjoint_step(l_old, l, c2, dt2, dx, dy, k, source=None):
+    """Adjoint step ``l+ = 2l - l- + dt^2 lap(c^2 l) + s``, then the forward Mur.
+
+    Restates _advance_adjoint_field_batch (fdtd2d/torch_backend.py:525-537) and
+    the single-shot adjoint branch of _advance_field (201-205): the adjoint
+    reuses the forward Mur update, which is not its exact transpose
+    (fdtd2d/inversion/gradient.py:9-11).
+    """
+    l_next = 2.0 * l - l_old + dt2 * laplacian(c2 * l, dx, dy)
+    if source is not None:
+        l_next = l_next + source
+    return apply_mur(l, l_next, k)
+
+
+# ---------------------------------------------------------------------------
+# Receivers and sources
+# ---------------------------------------------------------------------------
+
+def gather(fields, geo):
+    """Bilinear receiver samples ``(..., R)`` (fdtd2d/torch_backend.py:540-548)."""
+    return (
+        fields[..., geo["row0"], geo["col0"]] * geo["w00"]
+        + fields[..., geo["row0"], geo["col1"]] * geo["w10"]
+        + fields[..., geo["row1"], geo["col0"]] * geo["w01"]
+        + fields[..., geo["row1"], geo["col1"]] * geo["w11"]
+    )
+
+
+def scatter(residual, geo, shape):
+    """Transpose of ``gather``: ``(S, R)`` residuals onto ``(S, ny, nx)``.
+
+    Restates _adjoint_inject_batch's four accumulating index_put_ calls
+    (fdtd2d/torch_backend.py:571-577) and RingArray.record_adjoint
+    (fdtd2d/array.py:87-105).
+    """
+    residual = np.asarray(residual)
+    out = np.zeros((residual.shape[0],) + tuple(shape), dtype=residual.dtype)
+    for s in range(residual.shape[0]):
+        for rows, cols, w in (("row0", "col0", "w00"), ("row0", "col1", "w10"),
+                              ("row1", "col0", "w01"), ("row1", "col1", "w11")):
+            np.add.at(out[s], (geo[rows], geo[cols]), residual[s] * geo[w])
+    return out
+
+
+def point_sources(shape, rows, cols, weights=None):
+    """Dense per-shot injection fields with one or more weighted nodes per shot.
+
+    Nearest-node injection (fdtd2d/torch_backend.py:517, ``u_next[b, row_b,
+    col_b] += value``) is one node of weight 1 per shot. The bilinear source of
+    desmond/src/phase2_numerics.py:107-118 is four nodes per shot with the
+    bilinear weights, added as a dense field (torch_backend.py:209-210).
+    ``rows``/``cols``/``weights`` are ``(S,)`` or ``(S, K)``.
+    """
+    rows = np.atleast_1d(np.asarray(rows))
+    cols = np.atleast_1d(np.asarray(cols))
+    if rows.ndim == 1:
+        rows = rows[:, None]
+        cols = cols[:, None]
+    if weights is None:
+        weights = np.ones(rows.shape)
+    weights = np.asarray(weights, dtype=float).reshape(rows.shape)
+    field = np.zeros((rows.shape[0],) + tuple(shape))
+    for s in range(rows.shape[0]):
+        np.add.at(field[s], (rows[s], cols[s]), weights[s])
+    return field
+
+
+def bilinear_source_taps(geo, tx):
+    """Rows, columns and weights of the 4-node bilinear source of element ``tx``.
+
+    Restates desmond/src/phase2_numerics.py:107-118, which spreads the point
+    source over the four surrounding nodes with the receiver weights.
+    """
+    rows = [geo["row0"][tx], geo["row0"][tx], geo["row1"][tx], geo["row1"][tx]]
+    cols = [geo["col0"][tx], geo["col1"][tx], geo["col0"][tx], geo["col1"][tx]]
+    w = [geo["w00"][tx], geo["w10"][tx], geo["w01"][tx], geo["w11"][tx]]
+    return np.array(rows), np.array(cols), np.array(w)
+
+
+# ---------------------------------------------------------------------------
+# Batched drivers (fdtd2d/torch_backend.py:736-770, invert_ring.py:422-455)
+# ---------------------------------------------------------------------------
+
+def simulate_shots_batch(c, dx, dy, dt, geo, source_fields, source_values, n_steps,
+                         store=False, dtype=np.float64):
+    """Batched forward run; returns traces ``(S, R, n_steps)`` and the final state.
+
+    Restates simulate_shots_batch (fdtd2d/torch_backend.py:736-770): every step
+    injects ``source_values[step] * source_fields`` (per-shot dense fields), applies
+    Mur and samples the receivers from the new field. ``source_values`` is
+    ``(n_steps,)`` (one waveform shared by all shots, as in the reference) or
+    ``(S, n_steps)``. With ``store=True`` also returns every field after every step
+    ``(n_steps, S, ny, nx)`` as forward_store_batch does with ``store_every=1``
+    (invert_ring.py:422-455).
+    """
+    c = np.asarray(c, dtype=dtype)
+    c2 = c * c
+    dt2 = dtype(dt) * dtype(dt)
+    k = mur_coefficients(c, dtype(dt), dtype(dx), dtype(dy))
+    source_fields = np.asarray(source_fields, dtype=dtype)
+    n_shots = source_fields.shape[0]
+    values = np.asarray(source_values, dtype=dtype)
+    if values.ndim == 1:
+        values = np.broadcast_to(values, (n_shots, values.shape[0]))
+    u_old = np.zeros((n_shots,) + c.shape, dtype=dtype)
+    u = np.zeros_like(u_old)
+    n_rx = len(geo["row0"])
+    traces = np.zeros((n_shots, n_rx, n_steps), dtype=dtype)
+    wave = np.zeros((n_steps,) + u.shape, dtype=dtype) if store else None
+    for step in range(n_steps):
+        src = source_fields * values[:, step, None, None] if step < values.shape[1] else None
+        u_next = forward_step(u_old, u, c2, dt2, dx, dy, k, src)
+        u_old, u = u, u_next
+        traces[:, :, step] = gather(u, geo)
+        if store:
+            wave[step] = u
+    return traces, u_old, u, wave
+
+
+def residual_batch(predicted, observed, mute):
+    """Residual with each shot's transmitter channel zeroed.
+
+    Restates TorchLeastSquaresFWI._residual_batch (invert_ring.py:603-609) and
+    fdtd2d/inversion/misfit.py:6-16. ``mute`` holds one channel per shot, or -1
+    for no muting (the arc geometry, invert_arc.py:294-307).
+    """
+    residual = np.array(predicted - observed, copy=True)
+    for s, ch in enumerate(np.asarray(mute)):
+        if ch >= 0:
+            residual[s, ch] = 0.0
+    return residual
+
+
+def adjoint_gradient_c2(c, dx, dy, dt, geo, wave, residual):
+    """Summed-over-shots gradient with respect to c^2 by the reverse-time loop.
+
+    Restates _adjoint_accumulate_batch with ``store_every = 1`` (invert_ring.py:
+    683-701) and the fused adjoint_step_image / adjoint_step_residual steps
+    (fdtd2d/torch_backend.py:563-598): at loop index n the residual column n is
+    scattered and injected, the adjoint field steps, and for n >= 1
+    ``g += dt^2 * sum_shots(l+ * lap(wave[n-1]))`` with the zero-padded Laplacian.
+    ``wave`` is ``(n_steps, S, ny, nx)``, ``residual`` ``(S, R, n_steps)``.
+    """
+    c = np.asarray(c, dtype=float)
+    c2 = c * c
+    dt2 = dt * dt
+    k = mur_coefficients(c, dt, dx, dy)
+    n_steps = residual.shape[2]
+    n_shots = residual.shape[0]
+    l_old = np.zeros((n_shots,) + c.shape)
+    lam = np.zeros_like(l_old)
+    g = np.zeros(c.shape)
+    for n in range(n_steps - 1, -1, -1):
+        src = scatter(residual[:, :, n], geo, c.shape)
+        l_next = adjoint_step(l_old, lam, c2, dt2, dx, dy, k, src)
+        l_old, lam = lam, l_next
+        if n > 0:
+            g += dt2 * np.sum(lam * laplacian(wave[n - 1], dx, dy), axis=0)
+    return g
+
+
+def misfit_and_gradient_c2(c, dx, dy, dt, geo, source_fields, source_values, n_steps,
+                           observed, mute):
+    """Misfit ``0.5 * sum(residual^2)`` and the unmasked ``g_{c^2}``.
+
+    The device part of TorchLeastSquaresFWI.misfit_and_grad (invert_ring.py:
+    634-656) for fixed shots with ``store_every = 1``, in float64.
+    """
+    traces, _, _, wave = simulate_shots_batch(
+        c, dx, dy, dt, geo, source_fields, source_values, n_steps, store=True)
+    residual = residual_batch(traces, observed, mute)
+    misfit = 0.5 * float(np.sum(residual * residual))
+    return misfit, adjoint_gradient_c2(c, dx, dy, dt, geo, wave, residual)
+
+
+def gradient_m(g_c2, m, mask=None):
+    """Chain rule to slowness squared ``g_m = -g_{c^2} / m^2``, zero off the mask.
+
+    Restates invert_ring.py:657-659 (without the regularisation terms).
+    """
+    g = -np.asarray(g_c2, dtype=float) / (np.asarray(m, float) ** 2)
+    if mask is not None:
+        g = np.where(mask, g, 0.0)
+    return g
+
+
+def interior_mask(x_m, y_m, radius_m, margin_m, center=(0.0, 0.0)):
+    """Pixels strictly inside ``radius - margin`` (fdtd2d/inversion/medium.py:28-40)."""
+    x, y = np.meshgrid(x_m, y_m, indexing="xy")
+    r = float(radius_m) - float(margin_m)
+    return (x - center[0]) ** 2 + (y - center[1]) ** 2 < r * r

@@ -1,0 +1,142 @@
+"""Pin the NumPy oracle against outputs of the reference itself.
+
+The fixtures in ``tests/golden`` were produced by running the reference's torch
+engine in float64 (``tests/golden/make_golden.py``). Agreement here is at the
+level of float64 rounding, so the oracle can stand in for the reference in the
+GPU parity tests.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import fdtd_oracle as orc
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a - b)) / np.linalg.norm(np.ravel(b)))
+
+
+def geo_from(d, prefix=""):
+    g = {k: d[prefix + k] for k in ("row0", "col0", "w00", "w10", "w01", "w11")}
+    g["row1"] = g["row0"] + 1
+    g["col1"] = g["col0"] + 1
+    return g
+
+
+def test_ring41_single_and_batched_traces(golden):
+    d = golden("ring41")
+    geo = geo_from(d)
+    shape = d["c_true"].shape
+    src = orc.point_sources(shape, d["rows"], d["cols"])
+    nt = int(d["n_steps"])
+    traces, _, u, _ = orc.simulate_shots_batch(
+        d["c_true"], float(d["dx"]), float(d["dy"]), float(d["dt"]), geo, src,
+        np.pad(d["pulse"], (0, nt - d["pulse"].size)), nt)
+    assert rel(traces, d["observed"]) < 1e-12
+    assert rel(traces, d["batched_traces"]) < 1e-12
+    assert rel(u, d["batched_u"]) < 1e-12
+
+
+def test_ring41_gradient_and_misfit(golden):
+    d = golden("ring41")
+    geo = geo_from(d)
+    shape = d["c_true"].shape
+    nt = int(d["n_steps"])
+    src = orc.point_sources(shape, d["rows"], d["cols"])
+    values = np.pad(d["pulse"], (0, nt - d["pulse"].size))
+    misfit, g_c2 = orc.misfit_and_gradient_c2(
+        d["c_m0"], float(d["dx"]), float(d["dy"]), float(d["dt"]), geo, src, values, nt,
+        d["observed"], np.arange(6))
+    assert rel(g_c2, d["g_c2"]) < 1e-10
+    assert misfit == pytest.approx(float(d["residual_misfit"]), rel=1e-12)
+    assert misfit == pytest.approx(float(d["misfit"]), rel=1e-12)
+    g_m = orc.gradient_m(g_c2, d["m0"], d["mask"])
+    assert rel(g_m, d["grad_m"]) < 1e-10
+
+
+def test_ellipse_traces_f64_and_reference_f32_drift(golden):
+    d = golden("ellipses64")
+    geo = geo_from(d)
+    n = d["c"].shape[0]
+    tx = d["tx"]
+    src = orc.point_sources((n, n), d["rows"][tx], d["cols"][tx])
+    nt = int(d["n_steps"])
+    traces, _, u, _ = orc.simulate_shots_batch(
+        d["c"], float(d["dx"]), float(d["dx"]), float(d["dt"]), geo, src, d["wavelet"], nt)
+    assert rel(traces, d["traces_f64"]) < 1e-12
+    assert rel(u, d["u_f64"]) < 1e-12
+    # the reference's own float32 path sits well inside the 1e-5 trace budget
+    assert rel(d["traces_f32"], d["traces_f64"]) < 1e-5
+
+
+def test_ellipse_gradient(golden):
+    d = golden("ellipses64")
+    geo = geo_from(d)
+    n = d["c"].shape[0]
+    tx = d["tx"]
+    nt = int(d["n_steps"])
+    dx, dt = float(d["dx"]), float(d["dt"])
+    src = orc.point_sources((n, n), d["rows"][tx], d["cols"][tx])
+    observed, _, _, _ = orc.simulate_shots_batch(d["c"], dx, dx, dt, geo, src, d["wavelet"], nt)
+    misfit, g_c2 = orc.misfit_and_gradient_c2(
+        d["c_start"], dx, dx, dt, geo, src, d["wavelet"], nt, observed, tx)
+    assert rel(g_c2, d["g_c2_tx"]) < 1e-9
+    assert misfit == pytest.approx(float(d["misfit_tx"]), rel=1e-10)
+
+
+def test_bilinear_source(golden):
+    d = golden("ellipses64")
+    geo = geo_from(d)
+    n = d["c"].shape[0]
+    tx = int(d["bilinear_tx"])
+    full = orc.ring_geometry(16, 0.45 * n * float(d["dx"]), orc.axis_centers(n, float(d["dx"])),
+                             orc.axis_centers(n, float(d["dx"])))
+    rows, cols, w = orc.bilinear_source_taps(full, tx)
+    src = orc.point_sources((n, n), rows[None], cols[None], w[None])
+    nt = int(d["n_steps"])
+    traces, _, _, _ = orc.simulate_shots_batch(
+        d["c"], float(d["dx"]), float(d["dx"]), float(d["dt"]), geo, src, d["wavelet"], nt)
+    assert rel(traces[0], d["bilinear_traces"]) < 1e-12
+
+
+def test_step_level_nonsquare(golden):
+    d = golden("steps_nonsquare")
+    geo = geo_from(d)
+    dx, dy, dt = float(d["dx"]), float(d["dy"]), float(d["dt"])
+    c = d["c"]
+    k = orc.mur_coefficients(c, dt, dx, dy)
+    c2 = c * c
+    src = orc.point_sources(c.shape, d["src_rows"], d["src_cols"]) * float(d["src_value"])
+    fwd = orc.forward_step(d["u_old0"], d["u0"], c2, dt * dt, dx, dy, k, src)
+    assert rel(fwd, d["fwd_u"]) < 1e-13
+    assert rel(orc.gather(fwd, geo), d["fwd_samples"]) < 1e-13
+    adj = orc.adjoint_step(d["u_old0"], d["u0"], c2, dt * dt, dx, dy, k,
+                           orc.scatter(d["resid"], geo, c.shape))
+    assert rel(adj, d["adj_u"]) < 1e-13
+    g = d["g_in"] + float(d["image_scale"]) * np.sum(adj * orc.laplacian(d["fwd_field"], dx, dy), 0)
+    assert rel(g, d["g_out"]) < 1e-13
+    single = orc.adjoint_step(d["u_old0"][0], d["u0"][0], c2, dt * dt, dx, dy, k, d["fwd_field"][0])
+    assert rel(single, d["single_adj"]) < 1e-13
+
+
+@pytest.mark.parametrize("n_cells", [256, 512, 1024])
+def test_ring_geometry(golden, n_cells):
+    d = golden("geometry")
+    n, h, n_el, radius = d[f"ring{n_cells}_meta"]
+    ax = orc.axis_centers(int(n), h)
+    g = orc.ring_geometry(int(n_el), radius, ax, ax)
+    for key in ("rows", "cols", "row0", "col0"):
+        np.testing.assert_array_equal(g[key], d[f"ring{n_cells}_{key}"])
+    for key in ("w00", "w10", "w01", "w11"):
+        np.testing.assert_allclose(g[key], d[f"ring{n_cells}_{key}"], rtol=0, atol=1e-14)
+
+
+def test_arc_geometry(golden):
+    d = golden("geometry")
+    n, h, n_el, radius, span, center = d["arc41_meta"]
+    ax = orc.axis_centers(int(n), h)
+    g = orc.arc_geometry(int(n_el), radius, span, center, ax, ax)
+    for key in ("rows", "cols", "row0", "col0"):
+        np.testing.assert_array_equal(g[key], d[f"arc41_{key}"])
+    for key in ("w00", "w10", "w01", "w11"):
+        np.testing.assert_allclose(g[key], d[f"arc41_{key}"], rtol=0, atol=1e-14)
