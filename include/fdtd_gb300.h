@@ -1,0 +1,247 @@
+/*
+ * fdtd_gb300.h -- C ABI of the GB300 (sm_103a) engine for the 2-D ring-array
+ * wave simulation and its adjoint-state FWI gradient.
+ *
+ * The reference (scjoshi/SoundWaveSimulation) is pure Python: its engine is
+ * fdtd2d/torch_backend.py and its gradient driver is TorchLeastSquaresFWI in
+ * invert_ring.py. It has no FFI of its own, so every entry point below names the
+ * reference function whose device work it replaces; the Python package
+ * soundwavesimulation_gb300 binds these symbols with ctypes and keeps the
+ * reference's class and method names on top of them.
+ *
+ * Conventions
+ *  - All functions return 0 (FDTD_OK) or an error code; fdtd_last_error() gives a
+ *    readable message for the calling thread.
+ *  - Fields are float32, shot-major (shots, ny, pitch) with row = y, column = x.
+ *    `pitch` is the row stride in elements: a multiple of 4 and >= nx. Columns
+ *    nx..pitch-1 are padding and must hold zeros.
+ *  - Traces and residuals are float32 (shots, receivers, steps), as the
+ *    reference returns them (fdtd2d/torch_backend.py:769).
+ *  - Pointers marked "device" are CUDA device pointers; "host" pointers are read
+ *    during the call only. `stream` is a cudaStream_t (NULL = legacy stream).
+ *  - No entry point allocates device memory: every device buffer, including the
+ *    engine workspace, is owned by the caller.
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDTD_ABI_VERSION 1
+
+enum {
+  FDTD_OK = 0,
+  FDTD_ERR_INVALID = 1,     /* bad argument (shape, range, CFL, ...) */
+  FDTD_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  FDTD_ERR_WORKSPACE = 3,   /* workspace missing or too small */
+  FDTD_ERR_UNSUPPORTED = 4, /* configuration outside what the kernels support */
+  FDTD_ERR_STATE = 5        /* call order violated (e.g. adjoint before forward) */
+};
+
+enum { FDTD_STORE_F32 = 0, FDTD_STORE_F16 = 1, FDTD_STORE_BF16 = 2 };
+
+/* Grid and medium. `coef` and `mur` come from fdtd_prepare_medium. */
+typedef struct fdtd_grid {
+  int32_t ny, nx, pitch;
+  double dx, dy, dt;
+  const float* coef; /* device (ny, pitch): (c * dt)^2 */
+  const float* mur;  /* device: k_left[ny], k_right[ny], k_bottom[nx], k_top[nx],
+                        corner_kx[4], corner_ky[4] (corners in the order
+                        (0,0), (0,nx-1), (ny-1,0), (ny-1,nx-1)) */
+} fdtd_grid;
+
+/* Bilinear receivers (host arrays of length n). Receiver i samples rows
+   row0[i], row0[i]+1 and columns col0[i], col0[i]+1 with weights
+   w[4i..4i+3] = (w00, w10, w01, w11) as in RingArray._init_bilinear
+   (fdtd2d/array.py:60-76). */
+typedef struct fdtd_receivers {
+  int32_t n;
+  const int32_t* row0;
+  const int32_t* col0;
+  const float* w;
+} fdtd_receivers;
+
+/* Soft sources: `per_shot` injection entries per shot (host arrays of shape
+   (n_shots, per_shot)); entry j of shot s adds w * waveforms[wave, step] to node
+   (row, col) before the Mur edges are applied. wave = -1 marks an unused entry.
+   Nearest-node injection (fdtd2d/torch_backend.py:517) is one entry of weight 1;
+   the bilinear source (desmond/src/phase2_numerics.py:107-118) is four. */
+typedef struct fdtd_sources {
+  int32_t per_shot;
+  const int32_t* row;
+  const int32_t* col;
+  const float* w;
+  const int32_t* wave;
+  const float* waveforms; /* device (n_waves, waveform_len) */
+  int32_t n_waves;
+  int32_t waveform_len;   /* samples per waveform; steps beyond it inject 0 */
+} fdtd_sources;
+
+typedef struct fdtd_problem {
+  fdtd_grid grid;
+  int32_t n_shots;
+  int32_t n_steps;
+  fdtd_receivers rx;
+  fdtd_sources src;
+} fdtd_problem;
+
+/* Launch shape of the temporally blocked engine. Zero fields take defaults. */
+typedef struct fdtd_tuning {
+  int32_t rows_per_lane;    /* rows each lane keeps in registers: 4 or 8 */
+  int32_t warps;            /* warps per CTA (region height = warps * rows_per_lane) */
+  int32_t steps_per_launch; /* leapfrog steps per HBM round trip (temporal block) */
+  int32_t ckpt_every;       /* checkpoint spacing in steps; 0 = about sqrt(2 nt) */
+  int32_t ckpt_store;       /* FDTD_STORE_F32 / _F16 / _BF16 */
+  int32_t ctas_per_sm;      /* persistent grid = SMs * ctas_per_sm; 0 = 1 */
+} fdtd_tuning;
+
+typedef struct fdtd_plan fdtd_plan; /* opaque host-side execution plan */
+
+/* ---------------------------------------------------------------- basics */
+int32_t fdtd_abi_version(void);
+const char* fdtd_last_error(void);
+
+/* Sound speed (device float64 (ny, nx), row stride nx) -> coef and Mur
+   coefficients, computed in float64 and rounded to float32.
+   Replaces TorchScalarWave2D.set_c (fdtd2d/torch_backend.py:158-168) and
+   TorchFDTD2D._refresh_boundaries (fdtd2d/torch_backend.py:264-275). */
+int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pitch,
+                            double dt, double dx, double dy,
+                            float* coef, float* mur, void* stream);
+
+/* ------------------------------------------------- one-step (plain) kernels */
+
+/* One leapfrog step for n_shots shots, Mur edges included:
+     forward: u_next = 2u - u_old + coef * lap(u) + sources
+     adjoint: u_next = 2u - u_old + lap(coef * u) + sources
+   Sources: `src_*` are device arrays of shape (n_shots, src_per_shot) (row, col,
+   weight, waveform index) and inject w * waveforms[wave * waveform_len + step];
+   `dense` (device (n_shots, ny, pitch), nullable) is added as a field.
+   u_next must not alias u_old or u.
+   Replaces _advance_field (fdtd2d/torch_backend.py:177-233),
+   _advance_field_batch (493-522) and _advance_adjoint_field_batch (525-537). */
+int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots,
+                  const float* u_old, const float* u, float* u_next,
+                  int32_t src_per_shot, const int32_t* src_row, const int32_t* src_col,
+                  const float* src_w, const int32_t* src_wave,
+                  const float* waveforms, int32_t waveform_len, int32_t step,
+                  const float* dense, int32_t adjoint, void* stream);
+
+/* Bilinear receiver samples of a field batch:
+   out[s * out_shot_stride + r * out_rx_stride] for s < n_shots, r < n_rx.
+   rx_rc is device int32 (n_rx, 2) = (row0, col0), rx_w device float (n_rx, 4).
+   Replaces _gather_receivers (fdtd2d/torch_backend.py:540-548) and
+   TorchRingSampler.record / record_batch (368-387). */
+int32_t fdtd_gather(const fdtd_grid* grid, int32_t n_shots, const float* fields,
+                    int32_t n_rx, const int32_t* rx_rc, const float* rx_w,
+                    float* out, int64_t out_shot_stride, int64_t out_rx_stride,
+                    void* stream);
+
+/* Transpose of fdtd_gather: writes, for every node in the receiver tap table,
+   dense[s, node] = sum of w * residual[s * res_shot_stride + rx * res_rx_stride]
+   over the taps that land on the node (a fixed order, so the result is
+   deterministic). Nodes outside the table are left untouched: zero `dense`
+   once, then reuse it. tap_nodes is device int32 (n_nodes, 10) =
+   (row, col, rx_0, ..., rx_7) with -1 for unused receivers, tap_w device
+   float (n_nodes, 8). fdtd_tap_table builds both.
+   Replaces the scatter of _adjoint_inject_batch (fdtd2d/torch_backend.py:563-577)
+   and TorchRingSampler.record_adjoint_batch (389-418). */
+int32_t fdtd_scatter(const fdtd_grid* grid, int32_t n_shots, int32_t n_nodes,
+                     const int32_t* tap_nodes, const float* tap_w,
+                     const float* residual, int64_t res_shot_stride, int64_t res_rx_stride,
+                     float* dense, void* stream);
+
+/* Imaging condition g[y, x] += scale * sum_s adj[s, y, x] * lap(fwd[s])[y, x]
+   with the zero-padded Laplacian at every node; g is float64 (ny, pitch).
+   Replaces the imaging term of _adjoint_image_batch (fdtd2d/torch_backend.py:
+   583-598). */
+int32_t fdtd_image(const fdtd_grid* grid, int32_t n_shots, const float* adj,
+                   const float* fwd, double scale, double* g, void* stream);
+
+/* Host helper: builds the deterministic receiver tap table used by
+   fdtd_scatter and the fused engine (unique nodes, up to 8 receivers each).
+   On input *n_nodes is the capacity of the output arrays (4 * n_rx suffices). */
+int32_t fdtd_tap_table(int32_t ny, int32_t nx, const fdtd_receivers* rx,
+                       int32_t* tap_nodes, float* tap_w, int32_t* n_nodes);
+
+/* ------------------------------------------------------- fused engine */
+
+/* Builds the host-side plan: tiling, tap and source tables, checkpoint
+   schedule and workspace layout. for_gradient = 1 reserves checkpoints,
+   the recompute segment buffer and the adjoint state. */
+int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
+                         int32_t for_gradient, fdtd_plan** plan);
+int32_t fdtd_plan_destroy(fdtd_plan* plan);
+int32_t fdtd_plan_workspace_bytes(const fdtd_plan* plan, size_t* bytes);
+/* Reports the resolved tuning (defaults filled in) and the checkpoint spacing. */
+int32_t fdtd_plan_tuning(const fdtd_plan* plan, fdtd_tuning* tuning);
+/* Binds a caller-owned device workspace (256-byte aligned) and uploads the
+   tables into it; synchronises `stream` once. */
+int32_t fdtd_plan_bind(fdtd_plan* plan, void* workspace, size_t bytes, void* stream);
+/* Updates the medium and source waveform pointers of a bound plan (same shapes). */
+int32_t fdtd_plan_set_medium(fdtd_plan* plan, const float* coef, const float* mur,
+                             const float* waveforms);
+
+/* Batched forward of every shot over n_steps with the fused temporally blocked
+   kernel. traces: device (n_shots, n_rx, n_steps). u_prev_out / u_out
+   (nullable, device (n_shots, ny, pitch)) receive the last two fields.
+   save_checkpoints = 1 keeps the checkpoints a later fdtd_adjoint needs.
+   Replaces simulate_shots_batch (fdtd2d/torch_backend.py:736-770) and
+   forward_store_batch (invert_ring.py:422-455). */
+int32_t fdtd_forward(fdtd_plan* plan, float* traces, float* u_prev_out, float* u_out,
+                     int32_t save_checkpoints, void* stream);
+
+/* Reverse-time adjoint of the last checkpointed forward: injects `residual`
+   (device (n_shots, n_rx, n_steps)), recomputes each checkpoint segment and
+   adds dt^2 * sum_{shots, n >= 1} adj^n * lap(u^{n-1}) into grad_c2 (device
+   float64 (ny, pitch)).
+   Replaces _adjoint_accumulate_batch (invert_ring.py:683-701) with
+   store_every = 1. */
+int32_t fdtd_adjoint(fdtd_plan* plan, const float* residual, double* grad_c2, void* stream);
+
+/* residual = traces - observed with channel mute[s] zeroed (mute[s] < 0: none),
+   misfit[0] += 0.5 * sum(residual^2) in float64. Arrays (n_shots, n_rx, n_steps);
+   residual may alias traces. observed_shot_stride lets `observed` be a row
+   subset of a larger gather. mute is device int32 (n_shots).
+   Replaces TorchLeastSquaresFWI._residual_batch and the misfit sum
+   (invert_ring.py:603-609, 651). */
+int32_t fdtd_residual_misfit(int32_t n_shots, int32_t n_rx, int32_t n_steps,
+                             const float* traces, const float* observed,
+                             int64_t observed_shot_stride, const int32_t* mute,
+                             float* residual, double* misfit, void* stream);
+
+/* g_m = -grad_c2 / m^2 where mask != 0, else 0 (float64, n elements, all device;
+   mask may be NULL). Replaces invert_ring.py:657-659 without regularisation. */
+int32_t fdtd_chain_rule(int64_t n, const double* grad_c2, const double* m,
+                        const uint8_t* mask, double* g_m, void* stream);
+
+/* ------------------------------------------------- plain per-shot engine */
+
+/* The plain form: each shot separately, one launch per step per kernel
+   (step, then gather), traces as fdtd_forward. Workspace: 3 fields of one shot.
+   Replaces simulate_shot (fdtd2d/torch_backend.py:443-474) looped over shots. */
+int32_t fdtd_forward_plain(const fdtd_problem* problem, float* traces,
+                           void* workspace, size_t bytes, void* stream);
+size_t fdtd_forward_plain_workspace(const fdtd_problem* problem);
+
+/* ------------------------------------------------------- tiling (host) */
+
+/* The 1-D tiler of the fused engine, exposed for tests: covers [0, n) with
+   regions of `region` cells whose origins are multiples of `align`, owned
+   ranges that partition [0, n) and lie at least `halo` cells inside interior
+   region borders, and keeps every domain edge row together with its inner
+   neighbour inside one band of `band` cells. out holds 4 ints per tile:
+   (region origin, owned begin, owned end, flags). */
+int32_t fdtd_tile_axis(int32_t n, int32_t region, int32_t align, int32_t halo,
+                       int32_t band, int32_t max_tiles, int32_t* out, int32_t* n_tiles);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDTD_GB300_H */

@@ -1,0 +1,162 @@
+// Device-side arithmetic and parameter blocks shared by every kernel of the
+// engine.
+//
+// All float32 arithmetic of the update is written with explicit round-to-nearest
+// intrinsics (no compiler contraction choices), so the one-step kernels, the
+// temporally blocked kernel and the checkpoint recompute produce bit-identical
+// fields, traces and Laplacians for the same inputs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fdtd {
+
+// ---------------------------------------------------------------- arithmetic
+
+// 5-point Laplacian (l + r) / dx^2 + (d + u) / dy^2 - 2 (1/dx^2 + 1/dy^2) c,
+// the conv2d kernel of fdtd2d/torch_backend.py:124-132.
+__device__ __forceinline__ float lap5(float c, float l, float r, float d, float u,
+                                      float idx2, float idy2, float cdiag) {
+  return __fmaf_rn(c, cdiag, __fmaf_rn(__fadd_rn(d, u), idy2, __fmul_rn(__fadd_rn(l, r), idx2)));
+}
+
+// Forward leapfrog 2u - u_old + (c dt)^2 lap(u)  (fdtd2d/torch_backend.py:516).
+__device__ __forceinline__ float leap(float c, float p, float coef, float lap) {
+  return __fmaf_rn(coef, lap, __fsub_rn(__fadd_rn(c, c), p));
+}
+
+// Adjoint leapfrog 2l - l_old + lap((c dt)^2 l)  (fdtd2d/torch_backend.py:531-532);
+// the coefficient is already inside the Laplacian operand.
+__device__ __forceinline__ float leap_adj(float c, float p, float lap) {
+  return __fadd_rn(__fsub_rn(__fadd_rn(c, c), p), lap);
+}
+
+// First-order Mur edge u_in + k (un_in - u_edge)  (fdtd2d/torch_backend.py:482-489).
+__device__ __forceinline__ float mur(float u_in, float k, float un_in, float u_edge) {
+  return __fmaf_rn(k, __fsub_rn(un_in, u_edge), u_in);
+}
+
+__device__ __forceinline__ float corner_avg(float fx, float fy) {
+  return __fmul_rn(0.5f, __fadd_rn(fx, fy));
+}
+
+// Bilinear receiver sample (fdtd2d/torch_backend.py:543-548).
+__device__ __forceinline__ float gather4(float a, float b, float c, float d,
+                                        float w00, float w10, float w01, float w11) {
+  return __fmaf_rn(d, w11, __fmaf_rn(c, w01, __fmaf_rn(b, w10, __fmul_rn(a, w00))));
+}
+
+// Accumulates one weighted injection term.
+__device__ __forceinline__ float inj_acc(float acc, float w, float v) {
+  return __fmaf_rn(w, v, acc);
+}
+
+__device__ __forceinline__ float inj_add(float un, float inj) { return __fadd_rn(un, inj); }
+
+// ------------------------------------------------------------ parameters
+
+constexpr int MODE_FWD = 0;  // forward: sources in, receiver traces out
+constexpr int MODE_REC = 1;  // recompute: sources in, Laplacian of every step out
+constexpr int MODE_ADJ = 2;  // adjoint: residual in, imaging into the gradient
+
+constexpr int RX = 128;       // region width: 32 lanes x 4 columns
+constexpr int SRC_MAX = 8;    // injection nodes per shot
+constexpr int TAP_C = 8;      // receivers sharing one tap node
+constexpr int SRC_C = 4;      // source entries sharing one node
+
+// Tile flags.
+constexpr int TF_LEFT = 1, TF_RIGHT = 2, TF_BOTTOM = 4, TF_TOP = 8, TF_OUTSIDE = 16;
+
+struct TbTile {
+  int rx0, ry0;          // region origin (rx0 multiple of 4)
+  int ox0, ox1, oy0, oy1;  // owned (written) cells
+  int flags;
+  int tap_off, ntap;     // receiver tap nodes inside the region
+  int rxl_off, nrxl;     // receivers with a tap inside the region
+  int rec_off, nrec;     // receivers whose samples this tile records
+  int pad0, pad1, pad2;
+};
+
+struct TbTap {           // one receiver tap node inside a tile
+  int packed;            // (thread << 8) | (row_in_lane * 4 + column_in_lane)
+  int rloc[TAP_C];       // tile-local receiver index of each contribution, -1 = none
+  float w[TAP_C];
+};
+
+struct TbRec {           // one receiver recorded by a tile
+  int rg;                // global receiver index
+  int slot[4];           // tile-local tap slots of (r0,c0), (r0,c1), (r1,c0), (r1,c1)
+  float w[4];
+};
+
+struct SrcNode {         // one injection node of one shot
+  int row, col;
+  int wave[SRC_C];       // waveform index per entry, -1 = none
+  float w[SRC_C];
+};
+
+struct TbParams {
+  // grid
+  int ny, nx, pitch;
+  float idx2, idy2, cdiag;
+  const float* coef;
+  const float* mur;
+  // tiling
+  const TbTile* tiles;
+  int ntiles, nshots, nwarps;
+  const TbTap* taps;
+  const int* rxl;
+  const TbRec* recs;
+  int ntap_max, nrxl_max, tmax;
+  // sources
+  const SrcNode* src;    // (nshots, SRC_MAX)
+  const int* nsrc;       // (nshots)
+  const float* waveforms;
+  int wave_len;
+  // state (nshots, ny, pitch)
+  const float* in_prev;
+  const float* in_cur;
+  float* out_prev;
+  float* out_cur;
+  // steps: FWD/REC n0 .. n0+nsteps-1, ADJ n0 .. n0-nsteps+1
+  int n0, nsteps;
+  // FWD
+  float* traces;
+  int nrx, nt;
+  // REC / ADJ
+  float* seg;
+  long long seg_stride;  // elements between consecutive steps of the segment buffer
+  int seg_base;          // step held in segment slot 0
+  const float* residual;
+  double* grad;
+  double scale;
+};
+
+// Dynamic shared-memory carve-up of the temporally blocked kernel; the host
+// sizes the launch with the same function.
+struct TbSmem {
+  size_t coef, g, xch, tap, res, src, mask, base, srcpos, total;
+};
+
+__host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+__host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int ntap_max,
+                                                 int nrxl_max, int tmax) {
+  TbSmem m;
+  const size_t region = size_t(nw) * ky * RX * sizeof(float);
+  size_t off = 0;
+  m.coef = off; off += region;
+  m.g = off; if (mode == MODE_ADJ) off += region;
+  m.xch = off; off += size_t(2) * nw * 2 * 32 * 16;
+  m.tap = off; off += tb_align16(size_t(tmax) * (ntap_max > 0 ? ntap_max : 1) * sizeof(float));
+  m.res = off; if (mode == MODE_ADJ) off += tb_align16(size_t(nrxl_max > 0 ? nrxl_max : 1) * tmax * sizeof(float));
+  m.src = off; off += tb_align16(size_t(tmax) * SRC_MAX * sizeof(float));
+  m.mask = off; off += size_t(nw) * 32 * sizeof(unsigned);
+  m.base = off; off += size_t(nw) * 32 * sizeof(int);
+  m.srcpos = off; off += SRC_MAX * sizeof(int);
+  m.total = tb_align16(off);
+  return m;
+}
+
+}  // namespace fdtd

@@ -1,0 +1,67 @@
+// Internal declarations shared by the translation units of the engine library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "fdtd_device.cuh"
+
+namespace fdtd {
+
+// Error state of the C ABI (per host thread).
+void set_error(const std::string& msg);
+int32_t fail(int32_t code, const std::string& msg);
+int32_t cuda_fail(cudaError_t e, const char* what);
+
+// Temporally blocked kernel (fdtd_tb.cu).
+cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st);
+
+// One-step kernels and helpers (fdtd_kernels.cu).
+struct StepArgs {
+  int ny, nx, pitch;
+  float idx2, idy2, cdiag;
+  const float* coef;
+  const float* mur;
+  int n_shots;
+  const float* u_old;
+  const float* u;
+  float* u_next;
+  int src_per_shot;
+  const int32_t* src_row;
+  const int32_t* src_col;
+  const float* src_w;
+  const int32_t* src_wave;
+  const float* waveforms;
+  int wave_len;
+  int step;
+  const float* dense;
+  int adjoint;
+};
+cudaError_t step_launch(const StepArgs& a, cudaStream_t st);
+cudaError_t gather_launch(int ny, int pitch, int n_shots, const float* fields, int n_rx,
+                          const int32_t* rx_rc, const float* rx_w, float* out,
+                          long long shot_stride, long long rx_stride, cudaStream_t st);
+cudaError_t scatter_launch(int ny, int pitch, int n_shots, int n_nodes, const int32_t* nodes,
+                           const float* w, const float* res, long long shot_stride,
+                           long long rx_stride, float* dense, cudaStream_t st);
+cudaError_t image_launch(int ny, int nx, int pitch, float idx2, float idy2, float cdiag,
+                         int n_shots, const float* adj, const float* fwd, double scale,
+                         double* g, cudaStream_t st);
+cudaError_t prepare_medium_launch(const double* c, int ny, int nx, int pitch, double dt,
+                                  double dx, double dy, float* coef, float* mur,
+                                  cudaStream_t st);
+cudaError_t residual_launch(int n_shots, int n_rx, int n_steps, const float* traces,
+                            const float* observed, long long obs_shot_stride,
+                            const int32_t* mute, float* residual, double* misfit,
+                            cudaStream_t st);
+cudaError_t chain_rule_launch(long long n, const double* g, const double* m,
+                              const uint8_t* mask, double* out, cudaStream_t st);
+// 16-bit checkpoint storage with one power-of-two scale per (field, shot).
+cudaError_t quantize_launch(const float* src, void* dst, float* scales, int n_shots,
+                            long long per_shot, int store, cudaStream_t st);
+cudaError_t dequantize_launch(const void* src, const float* scales, float* dst, int n_shots,
+                              long long per_shot, int store, cudaStream_t st);
+
+}  // namespace fdtd

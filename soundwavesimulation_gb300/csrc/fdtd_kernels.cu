@@ -1,0 +1,356 @@
+// One-step ("plain") kernels and small helpers: medium preparation, the
+// receiver gather / residual scatter, the imaging condition, the residual and
+// misfit, the chain rule, and 16-bit checkpoint (de)quantisation.
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "fdtd_internal.h"
+
+namespace fdtd {
+namespace {
+
+__device__ __forceinline__ float operand(const StepArgs& a, const float* u, int y, int x) {
+  if (y < 0 || y >= a.ny || x < 0 || x >= a.nx) return 0.f;
+  const long long i = (long long)y * a.pitch + x;
+  const float v = u[i];
+  return a.adjoint ? __fmul_rn(a.coef[i], v) : v;
+}
+
+// Interior update of node (y, x) of shot s, sources included, before Mur.
+__device__ float cell_next(const StepArgs& a, int s, int y, int x) {
+  const long long plane = (long long)a.ny * a.pitch;
+  const float* u = a.u + s * plane;
+  const float* uo = a.u_old + s * plane;
+  const long long i = (long long)y * a.pitch + x;
+  const float lap = lap5(operand(a, u, y, x), operand(a, u, y, x - 1), operand(a, u, y, x + 1),
+                         operand(a, u, y - 1, x), operand(a, u, y + 1, x), a.idx2, a.idy2, a.cdiag);
+  float un = a.adjoint ? leap_adj(u[i], uo[i], lap) : leap(u[i], uo[i], a.coef[i], lap);
+  if (a.src_per_shot > 0) {
+    float acc = 0.f;
+    bool hit = false;
+    for (int j = 0; j < a.src_per_shot; ++j) {
+      const int e = s * a.src_per_shot + j;
+      if (a.src_row[e] == y && a.src_col[e] == x && a.src_wave[e] >= 0) {
+        const float v = (a.step < a.wave_len)
+                            ? a.waveforms[(long long)a.src_wave[e] * a.wave_len + a.step]
+                            : 0.f;
+        acc = inj_acc(acc, a.src_w[e], v);
+        hit = true;
+      }
+    }
+    if (hit) un = inj_add(un, acc);
+  }
+  if (a.dense) un = inj_add(un, a.dense[s * plane + i]);
+  return un;
+}
+
+__global__ void step_kernel(const StepArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int s = blockIdx.z;
+  if (x >= a.nx || y >= a.ny) return;
+  const long long plane = (long long)a.ny * a.pitch;
+  const float* u = a.u + s * plane;
+  const int ny = a.ny, nx = a.nx, P = a.pitch;
+  const float* kl = a.mur;
+  const float* kr = kl + ny;
+  const float* kb = kr + ny;
+  const float* kt = kb + nx;
+  const float* ckx = kt + nx;
+  const float* cky = ckx + 4;
+  const bool bot = y == 0, top = y == ny - 1, lef = x == 0, rig = x == nx - 1;
+  float out;
+  if (!(bot || top || lef || rig)) {
+    out = cell_next(a, s, y, x);
+  } else if (!(lef || rig)) {  // row 0 or ny-1 (fdtd2d/torch_backend.py:218-223)
+    const int yi = bot ? 1 : ny - 2;
+    out = mur(u[yi * P + x], bot ? kb[x] : kt[x], cell_next(a, s, yi, x), u[y * P + x]);
+  } else if (!(bot || top)) {  // column 0 or nx-1 (fdtd2d/torch_backend.py:212-217)
+    const int xi = lef ? 1 : nx - 2;
+    out = mur(u[y * P + xi], lef ? kl[y] : kr[y], cell_next(a, s, y, xi), u[y * P + x]);
+  } else {  // corner from the updated edges (fdtd2d/torch_backend.py:225-232)
+    const int ci = (bot ? 0 : 2) + (lef ? 0 : 1);
+    const int yi = bot ? 1 : ny - 2, xi = lef ? 1 : nx - 2;
+    const float inner = cell_next(a, s, yi, xi);
+    const float ex = mur(u[yi * P + xi], bot ? kb[xi] : kt[xi], inner, u[y * P + xi]);
+    const float ey = mur(u[yi * P + xi], lef ? kl[yi] : kr[yi], inner, u[yi * P + x]);
+    const float fx = mur(u[y * P + xi], ckx[ci], ex, u[y * P + x]);
+    const float fy = mur(u[yi * P + x], cky[ci], ey, u[y * P + x]);
+    out = corner_avg(fx, fy);
+  }
+  a.u_next[s * plane + (long long)y * P + x] = out;
+}
+
+__global__ void gather_kernel(int pitch, long long plane, int n_shots, const float* f, int n_rx,
+                              const int32_t* rc, const float* w, float* out,
+                              long long shot_stride, long long rx_stride) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  if (r >= n_rx || s >= n_shots) return;
+  const int r0 = rc[2 * r], c0 = rc[2 * r + 1];
+  const float* fs = f + s * plane + (long long)r0 * pitch + c0;
+  out[s * shot_stride + r * rx_stride] =
+      gather4(fs[0], fs[1], fs[pitch], fs[pitch + 1], w[4 * r], w[4 * r + 1], w[4 * r + 2], w[4 * r + 3]);
+}
+
+__global__ void scatter_kernel(int pitch, long long plane, int n_shots, int n_nodes,
+                               const int32_t* nodes, const float* w, const float* res,
+                               long long shot_stride, long long rx_stride, float* dense) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  if (i >= n_nodes || s >= n_shots) return;
+  const int32_t* nd = nodes + (long long)i * (2 + TAP_C);
+  float acc = 0.f;
+#pragma unroll
+  for (int q = 0; q < TAP_C; ++q) {
+    const int rid = nd[2 + q];
+    if (rid >= 0) acc = inj_acc(acc, w[(long long)i * TAP_C + q], res[s * shot_stride + rid * rx_stride]);
+  }
+  dense[s * plane + (long long)nd[0] * pitch + nd[1]] = acc;
+}
+
+__device__ __forceinline__ float at0(const float* f, int ny, int nx, int pitch, int y, int x) {
+  return (y >= 0 && y < ny && x >= 0 && x < nx) ? f[(long long)y * pitch + x] : 0.f;
+}
+
+__global__ void image_kernel(int ny, int nx, int pitch, float idx2, float idy2, float cdiag,
+                             int n_shots, const float* adj, const float* fwd, double scale,
+                             double* g) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= nx || y >= ny) return;
+  const long long plane = (long long)ny * pitch;
+  float acc = 0.f;
+  for (int s = 0; s < n_shots; ++s) {
+    const float* f = fwd + s * plane;
+    const float lap = lap5(at0(f, ny, nx, pitch, y, x), at0(f, ny, nx, pitch, y, x - 1),
+                           at0(f, ny, nx, pitch, y, x + 1), at0(f, ny, nx, pitch, y - 1, x),
+                           at0(f, ny, nx, pitch, y + 1, x), idx2, idy2, cdiag);
+    acc = __fmaf_rn(adj[s * plane + (long long)y * pitch + x], lap, acc);
+  }
+  g[(long long)y * pitch + x] += (double)acc * scale;
+}
+
+__device__ __forceinline__ double mur_k(double c, double dt, double h) {
+  return (c * dt - h) / (c * dt + h);
+}
+
+__global__ void coef_kernel(const double* c, int ny, int nx, int pitch, double dt, float* coef) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= pitch || y >= ny) return;
+  float v = 0.f;
+  if (x < nx) {
+    const double cd = c[(long long)y * nx + x] * dt;
+    v = (float)(cd * cd);
+  }
+  coef[(long long)y * pitch + x] = v;
+}
+
+__global__ void mur_kernel(const double* c, int ny, int nx, double dt, double dx, double dy,
+                           float* mur) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float* kl = mur;
+  float* kr = kl + ny;
+  float* kb = kr + ny;
+  float* kt = kb + nx;
+  float* ckx = kt + nx;
+  float* cky = ckx + 4;
+  if (i < ny) {
+    const bool in = i >= 1 && i <= ny - 2;
+    kl[i] = in ? (float)mur_k(c[(long long)i * nx], dt, dx) : 0.f;
+    kr[i] = in ? (float)mur_k(c[(long long)i * nx + nx - 1], dt, dx) : 0.f;
+  }
+  if (i < nx) {
+    const bool in = i >= 1 && i <= nx - 2;
+    kb[i] = in ? (float)mur_k(c[i], dt, dy) : 0.f;
+    kt[i] = in ? (float)mur_k(c[(long long)(ny - 1) * nx + i], dt, dy) : 0.f;
+  }
+  if (i < 4) {
+    const int r = (i < 2) ? 0 : ny - 1;
+    const int col = (i & 1) ? nx - 1 : 0;
+    const double cc = c[(long long)r * nx + col];
+    ckx[i] = (float)mur_k(cc, dt, dx);
+    cky[i] = (float)mur_k(cc, dt, dy);
+  }
+}
+
+__global__ void residual_kernel(long long total, long long per_shot, int n_steps,
+                                const float* traces, const float* obs, long long obs_stride,
+                                const int32_t* mute, float* res, double* misfit) {
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long s = i / per_shot;
+    const long long rem = i - s * per_shot;
+    const int r = (int)(rem / n_steps);
+    float v = __fsub_rn(traces[i], obs[s * obs_stride + rem]);
+    if (mute && mute[s] == r) v = 0.f;
+    res[i] = v;
+    acc += (double)v * (double)v;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  __shared__ double part[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) part[wid] = acc;
+  __syncthreads();
+  if (wid == 0) {
+    acc = (lane < (int)(blockDim.x >> 5)) ? part[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) atomicAdd(misfit, 0.5 * acc);
+  }
+}
+
+__global__ void chain_kernel(long long n, const double* g, const double* m, const uint8_t* mask,
+                             double* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    out[i] = (mask && !mask[i]) ? 0.0 : -g[i] / (m[i] * m[i]);
+  }
+}
+
+__global__ void amax_kernel(const float* src, long long per_shot, unsigned* amax) {
+  const int s = blockIdx.y;
+  float a = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_shot;
+       i += (long long)gridDim.x * blockDim.x) {
+    a = fmaxf(a, fabsf(src[s * per_shot + i]));
+  }
+  for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_down_sync(0xffffffffu, a, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(amax + s, __float_as_uint(a));
+}
+
+// Power-of-two scale that maps the largest magnitude to at most 2^15.
+__device__ __forceinline__ float pow2_scale(unsigned amax_bits) {
+  const float a = __uint_as_float(amax_bits);
+  if (!(a > 0.f) || !isfinite(a)) return 1.f;
+  int e;
+  frexpf(a, &e);  // a = f * 2^e, f in [0.5, 1)
+  return ldexpf(1.f, e - 15);
+}
+
+__global__ void quant_kernel(const float* src, void* dst, const unsigned* amax, float* scales,
+                             long long per_shot, int store) {
+  const int s = blockIdx.y;
+  const float sc = pow2_scale(amax[s]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) scales[s] = sc;
+  const float inv = 1.f / sc;  // exact: sc is a power of two
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_shot;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float v = src[s * per_shot + i] * inv;
+    if (store == 1) {
+      reinterpret_cast<__half*>(dst)[s * per_shot + i] = __float2half_rn(v);
+    } else {
+      reinterpret_cast<__nv_bfloat16*>(dst)[s * per_shot + i] = __float2bfloat16_rn(v);
+    }
+  }
+}
+
+__global__ void dequant_kernel(const void* src, const float* scales, float* dst,
+                               long long per_shot, int store) {
+  const int s = blockIdx.y;
+  const float sc = scales[s];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_shot;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float q = (store == 1) ? __half2float(reinterpret_cast<const __half*>(src)[s * per_shot + i])
+                                 : __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(src)[s * per_shot + i]);
+    dst[s * per_shot + i] = q * sc;
+  }
+}
+
+}  // namespace
+
+cudaError_t step_launch(const StepArgs& a, cudaStream_t st) {
+  dim3 block(32, 8);
+  dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8, a.n_shots);
+  step_kernel<<<grid, block, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t gather_launch(int ny, int pitch, int n_shots, const float* fields, int n_rx,
+                          const int32_t* rx_rc, const float* rx_w, float* out,
+                          long long shot_stride, long long rx_stride, cudaStream_t st) {
+  dim3 grid((n_rx + 127) / 128, n_shots);
+  gather_kernel<<<grid, 128, 0, st>>>(pitch, (long long)ny * pitch, n_shots, fields, n_rx, rx_rc,
+                                      rx_w, out, shot_stride, rx_stride);
+  return cudaGetLastError();
+}
+
+cudaError_t scatter_launch(int ny, int pitch, int n_shots, int n_nodes, const int32_t* nodes,
+                           const float* w, const float* res, long long shot_stride,
+                           long long rx_stride, float* dense, cudaStream_t st) {
+  dim3 grid((n_nodes + 127) / 128, n_shots);
+  scatter_kernel<<<grid, 128, 0, st>>>(pitch, (long long)ny * pitch, n_shots, n_nodes, nodes, w,
+                                       res, shot_stride, rx_stride, dense);
+  return cudaGetLastError();
+}
+
+cudaError_t image_launch(int ny, int nx, int pitch, float idx2, float idy2, float cdiag,
+                         int n_shots, const float* adj, const float* fwd, double scale,
+                         double* g, cudaStream_t st) {
+  dim3 block(32, 8);
+  dim3 grid((nx + 31) / 32, (ny + 7) / 8);
+  image_kernel<<<grid, block, 0, st>>>(ny, nx, pitch, idx2, idy2, cdiag, n_shots, adj, fwd,
+                                       scale, g);
+  return cudaGetLastError();
+}
+
+cudaError_t prepare_medium_launch(const double* c, int ny, int nx, int pitch, double dt,
+                                  double dx, double dy, float* coef, float* mur,
+                                  cudaStream_t st) {
+  dim3 block(32, 8);
+  dim3 grid((pitch + 31) / 32, (ny + 7) / 8);
+  coef_kernel<<<grid, block, 0, st>>>(c, ny, nx, pitch, dt, coef);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int n = (ny > nx ? ny : nx);
+  mur_kernel<<<(n + 255) / 256, 256, 0, st>>>(c, ny, nx, dt, dx, dy, mur);
+  return cudaGetLastError();
+}
+
+cudaError_t residual_launch(int n_shots, int n_rx, int n_steps, const float* traces,
+                            const float* observed, long long obs_shot_stride,
+                            const int32_t* mute, float* residual, double* misfit,
+                            cudaStream_t st) {
+  const long long per_shot = (long long)n_rx * n_steps;
+  const long long total = per_shot * n_shots;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  if (blocks < 1) blocks = 1;
+  residual_kernel<<<(int)blocks, 256, 0, st>>>(total, per_shot, n_steps, traces, observed,
+                                               obs_shot_stride, mute, residual, misfit);
+  return cudaGetLastError();
+}
+
+cudaError_t chain_rule_launch(long long n, const double* g, const double* m,
+                              const uint8_t* mask, double* out, cudaStream_t st) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  if (blocks < 1) blocks = 1;
+  chain_kernel<<<(int)blocks, 256, 0, st>>>(n, g, m, mask, out);
+  return cudaGetLastError();
+}
+
+cudaError_t quantize_launch(const float* src, void* dst, float* scales, int n_shots,
+                            long long per_shot, int store, cudaStream_t st) {
+  // scales holds 2 * n_shots floats: [0, n) amax scratch, [n, 2n) the scales.
+  unsigned* amax = reinterpret_cast<unsigned*>(scales);
+  cudaError_t e = cudaMemsetAsync(amax, 0, sizeof(unsigned) * n_shots, st);
+  if (e != cudaSuccess) return e;
+  dim3 grid(64, n_shots);
+  amax_kernel<<<grid, 256, 0, st>>>(src, per_shot, amax);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  quant_kernel<<<grid, 256, 0, st>>>(src, dst, amax, scales + n_shots, per_shot, store);
+  return cudaGetLastError();
+}
+
+cudaError_t dequantize_launch(const void* src, const float* scales, float* dst, int n_shots,
+                              long long per_shot, int store, cudaStream_t st) {
+  dim3 grid(64, n_shots);
+  dequant_kernel<<<grid, 256, 0, st>>>(src, scales + n_shots, dst, per_shot, store);
+  return cudaGetLastError();
+}
+
+}  // namespace fdtd

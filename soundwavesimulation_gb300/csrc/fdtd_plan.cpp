@@ -1,0 +1,856 @@
+// Host runtime of the engine: tiling, tap and source tables, checkpoint
+// schedule, workspace layout, the time-loop executors and the C ABI.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/fdtd_gb300.h"
+#include "fdtd_internal.h"
+
+namespace fdtd {
+
+static thread_local std::string g_error;
+
+void set_error(const std::string& msg) { g_error = msg; }
+
+int32_t fail(int32_t code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+int32_t cuda_fail(cudaError_t e, const char* what) {
+  return fail(FDTD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+constexpr size_t ALIGN = 256;
+constexpr size_t SMEM_LIMIT = 232448;  // 227 KB opt-in shared memory per CTA
+
+size_t align_up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
+
+struct AxisTile {
+  int origin, own0, own1, flags;  // flags: 1 low edge, 2 high edge, 4 outside cells
+};
+
+bool band_ok(int n, int origin, int region, int band) {
+  if (band <= 1) return true;
+  const int end = origin + region;
+  if (origin <= 0 && 0 < end) {
+    const int l = -origin;
+    if (l % band == band - 1) return false;  // row 0 and row 1 would sit in different bands
+  }
+  if (origin <= n - 1 && n - 1 < end) {
+    const int l = n - 1 - origin;
+    if (l % band == 0) return false;  // row n-1 and row n-2 would sit in different bands
+  }
+  return true;
+}
+
+int floor_align(int v, int a) {
+  if (a <= 1) return v;
+  return (v >= 0) ? (v / a) * a : -(((-v) + a - 1) / a) * a;
+}
+
+// Greedy 1-D tiling; see fdtd_tile_axis in the public header.
+std::string tile_axis(int n, int region, int align, int halo, int band, std::vector<AxisTile>& out) {
+  out.clear();
+  if (n < 4) return "grid axis must have at least 4 cells";
+  if (region <= 2 * halo + 1) return "region too small for the temporal halo";
+  int own0 = 0;
+  while (own0 < n) {
+    int origin = (own0 == 0) ? 0 : floor_align(own0 - halo, align);
+    if (origin < 0 && align > 1) origin = 0;
+    int tries = 0;
+    while (!band_ok(n, origin, region, band)) {
+      origin -= (align > 1 ? align : 1);
+      if (++tries > 64) return "no region placement satisfies the band constraint";
+    }
+    const int end = origin + region;
+    int own1 = (end >= n) ? n : end - halo;
+    if (origin > 0 && own0 < origin + halo) return "tiler produced an unsafe low border";
+    if (own1 <= own0) return "region too small to make progress";
+    AxisTile t;
+    t.origin = origin;
+    t.own0 = own0;
+    t.own1 = own1;
+    t.flags = (origin <= 0 ? 1 : 0) | (end >= n ? 2 : 0) | ((origin < 0 || end > n) ? 4 : 0);
+    out.push_back(t);
+    own0 = own1;
+    if (out.size() > 100000) return "too many tiles";
+  }
+  return "";
+}
+
+}  // namespace
+}  // namespace fdtd
+
+using namespace fdtd;
+
+struct fdtd_plan {
+  fdtd_problem prob;
+  fdtd_tuning tun;
+  int for_gradient = 0;
+  int ky = 8, nw = 16, tmax = 12, RY = 128;
+  std::vector<TbTile> tiles;
+  std::vector<TbTap> taps;
+  std::vector<int> rxl;
+  std::vector<TbRec> recs;
+  std::vector<SrcNode> src;
+  std::vector<int> nsrc;
+  int ntap_max = 0, nrxl_max = 0;
+  int ckpt_every = 0, nseg = 1;
+  size_t field_elems = 0;
+  // workspace offsets
+  size_t o_tiles = 0, o_taps = 0, o_rxl = 0, o_recs = 0, o_src = 0, o_nsrc = 0;
+  size_t o_state[2][2] = {{0, 0}, {0, 0}};
+  size_t o_adj[2][2] = {{0, 0}, {0, 0}};
+  size_t o_ckpt = 0, ckpt_elem_bytes = 4, o_scales = 0, o_seg = 0;
+  size_t total = 0;
+  size_t smem[3] = {0, 0, 0};
+  // binding
+  char* ws = nullptr;
+  size_t ws_bytes = 0;
+  bool bound = false;
+  bool have_ckpt = false;
+  int sm_count = 0;
+};
+
+namespace {
+
+int32_t validate_grid(const fdtd_grid& g) {
+  if (g.ny < 8 || g.nx < 8) return fail(FDTD_ERR_INVALID, "grid must be at least 8 x 8");
+  if (g.pitch < g.nx || g.pitch % 4 != 0) return fail(FDTD_ERR_INVALID, "pitch must be a multiple of 4 and >= nx");
+  if (!(g.dx > 0) || !(g.dy > 0) || !(g.dt > 0)) return fail(FDTD_ERR_INVALID, "dx, dy and dt must be positive");
+  if (!g.coef || !g.mur) return fail(FDTD_ERR_INVALID, "coef and mur must be set");
+  return FDTD_OK;
+}
+
+void fill_params(const fdtd_plan* p, TbParams& q) {
+  std::memset(&q, 0, sizeof(q));
+  const fdtd_grid& g = p->prob.grid;
+  q.ny = g.ny;
+  q.nx = g.nx;
+  q.pitch = g.pitch;
+  const double idx2 = 1.0 / (g.dx * g.dx), idy2 = 1.0 / (g.dy * g.dy);
+  q.idx2 = (float)idx2;
+  q.idy2 = (float)idy2;
+  q.cdiag = (float)(-2.0 * (idx2 + idy2));
+  q.coef = g.coef;
+  q.mur = g.mur;
+  q.tiles = reinterpret_cast<const TbTile*>(p->ws + p->o_tiles);
+  q.ntiles = (int)p->tiles.size();
+  q.nshots = p->prob.n_shots;
+  q.nwarps = p->nw;
+  q.taps = reinterpret_cast<const TbTap*>(p->ws + p->o_taps);
+  q.rxl = reinterpret_cast<const int*>(p->ws + p->o_rxl);
+  q.recs = reinterpret_cast<const TbRec*>(p->ws + p->o_recs);
+  q.ntap_max = p->ntap_max;
+  q.nrxl_max = p->nrxl_max;
+  q.tmax = p->tmax;
+  q.src = reinterpret_cast<const SrcNode*>(p->ws + p->o_src);
+  q.nsrc = reinterpret_cast<const int*>(p->ws + p->o_nsrc);
+  q.waveforms = p->prob.src.waveforms;
+  q.wave_len = p->prob.src.waveform_len;
+  q.nrx = p->prob.rx.n;
+  q.nt = p->prob.n_steps;
+  q.seg_stride = (long long)p->field_elems;
+}
+
+int grid_size(const fdtd_plan* p) {
+  const int items = (int)p->tiles.size() * p->prob.n_shots;
+  const int per_sm = p->tun.ctas_per_sm > 0 ? p->tun.ctas_per_sm : 1;
+  const int g = p->sm_count * per_sm;
+  return std::max(1, std::min(items, g));
+}
+
+float* fptr(fdtd_plan* p, size_t off) { return reinterpret_cast<float*>(p->ws + off); }
+
+int32_t launch(fdtd_plan* p, TbParams& q, int mode, cudaStream_t st) {
+  cudaError_t e = tb_launch(q, p->ky, mode, grid_size(p), p->smem[mode], st);
+  if (e != cudaSuccess) return cuda_fail(e, "temporally blocked kernel launch");
+  return FDTD_OK;
+}
+
+int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
+  const fdtd_grid& g = prob->grid;
+  const int ny = g.ny, nx = g.nx, KY = p->ky, RY = p->RY;
+  const int halo = p->tmax + 1;
+  std::vector<AxisTile> tx, ty;
+  std::string err = tile_axis(nx, RX, 4, halo, 0, tx);
+  if (!err.empty()) return fail(FDTD_ERR_UNSUPPORTED, "x tiling: " + err);
+  err = tile_axis(ny, RY, 1, halo, KY, ty);
+  if (!err.empty()) return fail(FDTD_ERR_UNSUPPORTED, "y tiling: " + err);
+
+  // receivers -> unique tap nodes, contributions in the reference's
+  // index_put_ order (all w00 taps, then w10, w01, w11)
+  const int R = prob->rx.n;
+  std::map<std::pair<int, int>, int> node_id;
+  std::vector<std::pair<int, int>> nodes;
+  std::vector<std::vector<std::pair<int, float>>> contrib;
+  for (int tap = 0; tap < 4; ++tap) {
+    for (int r = 0; r < R; ++r) {
+      const int r0 = prob->rx.row0[r], c0 = prob->rx.col0[r];
+      const int row = r0 + (tap >= 2 ? 1 : 0), col = c0 + (tap & 1);
+      auto key = std::make_pair(row, col);
+      auto it = node_id.find(key);
+      int id;
+      if (it == node_id.end()) {
+        id = (int)nodes.size();
+        node_id[key] = id;
+        nodes.push_back(key);
+        contrib.emplace_back();
+      } else {
+        id = it->second;
+      }
+      contrib[id].push_back({r, prob->rx.w[4 * r + tap]});
+      if ((int)contrib[id].size() > TAP_C) return fail(FDTD_ERR_UNSUPPORTED, "more than 8 receiver taps share one grid node");
+    }
+  }
+  for (int r = 0; r < R; ++r) {
+    const int r0 = prob->rx.row0[r], c0 = prob->rx.col0[r];
+    if (r0 < 0 || r0 > ny - 2 || c0 < 0 || c0 > nx - 2)
+      return fail(FDTD_ERR_INVALID, "receiver " + std::to_string(r) + " lies outside the grid");
+  }
+
+  p->tiles.clear();
+  p->taps.clear();
+  p->rxl.clear();
+  p->recs.clear();
+  p->ntap_max = 0;
+  p->nrxl_max = 0;
+  std::vector<int> recorded(R, 0);
+  for (const AxisTile& ay : ty) {
+    for (const AxisTile& ax : tx) {
+      TbTile t;
+      std::memset(&t, 0, sizeof(t));
+      t.rx0 = ax.origin;
+      t.ry0 = ay.origin;
+      t.ox0 = ax.own0;
+      t.ox1 = ax.own1;
+      t.oy0 = ay.own0;
+      t.oy1 = ay.own1;
+      t.flags = ((ax.flags & 1) ? TF_LEFT : 0) | ((ax.flags & 2) ? TF_RIGHT : 0) |
+                ((ay.flags & 1) ? TF_BOTTOM : 0) | ((ay.flags & 2) ? TF_TOP : 0) |
+                (((ax.flags | ay.flags) & 4) ? TF_OUTSIDE : 0);
+      if ((t.flags & TF_LEFT) && t.rx0 != 0) return fail(FDTD_ERR_UNSUPPORTED, "left edge tile must start at column 0");
+      // taps inside the region, sorted by (thread, bit)
+      std::vector<std::pair<int, int>> local;  // (packed, node id)
+      for (size_t id = 0; id < nodes.size(); ++id) {
+        const int ly = nodes[id].first - t.ry0, lx = nodes[id].second - t.rx0;
+        if (ly < 0 || ly >= RY || lx < 0 || lx >= RX) continue;
+        const int packed = (((ly / KY) * 32 + (lx >> 2)) << 8) | ((ly % KY) * 4 + (lx & 3));
+        local.push_back({packed, (int)id});
+      }
+      std::sort(local.begin(), local.end());
+      std::map<int, int> rloc;
+      std::vector<int> rx_here;
+      for (auto& pr : local)
+        for (auto& cw : contrib[pr.second])
+          if (!rloc.count(cw.first)) { rloc[cw.first] = 0; }
+      for (auto& kv : rloc) { kv.second = (int)rx_here.size(); rx_here.push_back(kv.first); }
+      t.tap_off = (int)p->taps.size();
+      t.ntap = (int)local.size();
+      std::map<int, int> slot_of_node;
+      for (size_t i = 0; i < local.size(); ++i) {
+        TbTap tp;
+        tp.packed = local[i].first;
+        for (int q = 0; q < TAP_C; ++q) { tp.rloc[q] = -1; tp.w[q] = 0.f; }
+        const auto& cl = contrib[local[i].second];
+        for (size_t q = 0; q < cl.size(); ++q) {
+          tp.rloc[q] = rloc[cl[q].first];
+          tp.w[q] = cl[q].second;
+        }
+        p->taps.push_back(tp);
+        slot_of_node[local[i].second] = (int)i;
+      }
+      t.rxl_off = (int)p->rxl.size();
+      t.nrxl = (int)rx_here.size();
+      p->rxl.insert(p->rxl.end(), rx_here.begin(), rx_here.end());
+      t.rec_off = (int)p->recs.size();
+      for (int r = 0; r < R; ++r) {
+        const int r0 = prob->rx.row0[r], c0 = prob->rx.col0[r];
+        if (r0 < t.oy0 || r0 >= t.oy1 || c0 < t.ox0 || c0 >= t.ox1) continue;
+        TbRec rc;
+        rc.rg = r;
+        for (int tap = 0; tap < 4; ++tap) {
+          const int id = node_id[{r0 + (tap >= 2 ? 1 : 0), c0 + (tap & 1)}];
+          auto it = slot_of_node.find(id);
+          if (it == slot_of_node.end()) return fail(FDTD_ERR_UNSUPPORTED, "receiver footprint outside its tile");
+          rc.slot[tap] = it->second;
+          rc.w[tap] = prob->rx.w[4 * r + tap];
+        }
+        p->recs.push_back(rc);
+        recorded[r]++;
+      }
+      t.nrec = (int)p->recs.size() - t.rec_off;
+      p->ntap_max = std::max(p->ntap_max, t.ntap);
+      p->nrxl_max = std::max(p->nrxl_max, t.nrxl);
+      p->tiles.push_back(t);
+    }
+  }
+  for (int r = 0; r < R; ++r)
+    if (recorded[r] != 1) return fail(FDTD_ERR_UNSUPPORTED, "receiver not recorded exactly once");
+
+  // per-shot injection nodes, duplicates merged in entry order
+  const int S = prob->n_shots, K = prob->src.per_shot;
+  p->src.assign((size_t)S * SRC_MAX, SrcNode());
+  p->nsrc.assign(S, 0);
+  for (int s = 0; s < S; ++s) {
+    int cnt = 0;
+    for (int j = 0; j < K; ++j) {
+      const int e = s * K + j;
+      if (prob->src.wave[e] < 0) continue;
+      const int row = prob->src.row[e], col = prob->src.col[e];
+      if (row < 0 || row >= ny || col < 0 || col >= nx) return fail(FDTD_ERR_INVALID, "source outside the grid");
+      if (prob->src.wave[e] >= prob->src.n_waves) return fail(FDTD_ERR_INVALID, "source waveform index out of range");
+      int found = -1;
+      for (int m = 0; m < cnt; ++m) {
+        const SrcNode& sn = p->src[(size_t)s * SRC_MAX + m];
+        if (sn.row == row && sn.col == col) found = m;
+      }
+      if (found < 0) {
+        if (cnt >= SRC_MAX) return fail(FDTD_ERR_UNSUPPORTED, "more than 8 source nodes in one shot");
+        SrcNode& sn = p->src[(size_t)s * SRC_MAX + cnt];
+        sn.row = row;
+        sn.col = col;
+        for (int q = 0; q < SRC_C; ++q) { sn.wave[q] = -1; sn.w[q] = 0.f; }
+        found = cnt++;
+      }
+      SrcNode& sn = p->src[(size_t)s * SRC_MAX + found];
+      int q = 0;
+      while (q < SRC_C && sn.wave[q] >= 0) ++q;
+      if (q == SRC_C) return fail(FDTD_ERR_UNSUPPORTED, "more than 4 source entries on one node");
+      sn.wave[q] = prob->src.wave[e];
+      sn.w[q] = prob->src.w[e];
+    }
+    p->nsrc[s] = cnt;
+  }
+  return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fdtd_abi_version(void) { return FDTD_ABI_VERSION; }
+
+const char* fdtd_last_error(void) { return g_error.c_str(); }
+
+int32_t fdtd_tile_axis(int32_t n, int32_t region, int32_t align, int32_t halo, int32_t band,
+                       int32_t max_tiles, int32_t* out, int32_t* n_tiles) {
+  std::vector<AxisTile> t;
+  std::string err = tile_axis(n, region, align, halo, band, t);
+  if (!err.empty()) return fail(FDTD_ERR_UNSUPPORTED, err);
+  if (n_tiles) *n_tiles = (int32_t)t.size();
+  if ((int)t.size() > max_tiles) return fail(FDTD_ERR_INVALID, "output too small");
+  for (size_t i = 0; i < t.size(); ++i) {
+    out[4 * i] = t[i].origin;
+    out[4 * i + 1] = t[i].own0;
+    out[4 * i + 2] = t[i].own1;
+    out[4 * i + 3] = t[i].flags;
+  }
+  return FDTD_OK;
+}
+
+int32_t fdtd_tap_table(int32_t ny, int32_t nx, const fdtd_receivers* rx, int32_t* tap_nodes,
+                       float* tap_w, int32_t* n_nodes) {
+  if (!rx || !n_nodes) return fail(FDTD_ERR_INVALID, "null argument");
+  std::map<std::pair<int, int>, int> node_id;
+  std::vector<std::pair<int, int>> nodes;
+  std::vector<std::vector<std::pair<int, float>>> contrib;
+  for (int tap = 0; tap < 4; ++tap) {
+    for (int r = 0; r < rx->n; ++r) {
+      const int row = rx->row0[r] + (tap >= 2 ? 1 : 0), col = rx->col0[r] + (tap & 1);
+      if (row < 0 || row >= ny || col < 0 || col >= nx) return fail(FDTD_ERR_INVALID, "receiver outside the grid");
+      auto key = std::make_pair(row, col);
+      auto it = node_id.find(key);
+      int id;
+      if (it == node_id.end()) {
+        id = (int)nodes.size();
+        node_id[key] = id;
+        nodes.push_back(key);
+        contrib.emplace_back();
+      } else {
+        id = it->second;
+      }
+      contrib[id].push_back({r, rx->w[4 * r + tap]});
+      if ((int)contrib[id].size() > TAP_C) return fail(FDTD_ERR_UNSUPPORTED, "more than 8 receiver taps share one grid node");
+    }
+  }
+  const int cap = *n_nodes;
+  *n_nodes = (int32_t)nodes.size();
+  if ((int)nodes.size() > cap) return fail(FDTD_ERR_INVALID, "tap table capacity too small");
+  for (size_t i = 0; i < nodes.size(); ++i) {
+    int32_t* nd = tap_nodes + i * (2 + TAP_C);
+    nd[0] = nodes[i].first;
+    nd[1] = nodes[i].second;
+    for (int q = 0; q < TAP_C; ++q) {
+      const bool used = q < (int)contrib[i].size();
+      nd[2 + q] = used ? contrib[i][q].first : -1;
+      tap_w[i * TAP_C + q] = used ? contrib[i][q].second : 0.f;
+    }
+  }
+  return FDTD_OK;
+}
+
+int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pitch, double dt,
+                            double dx, double dy, float* coef, float* mur, void* stream) {
+  if (!c || !coef || !mur) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (ny < 3 || nx < 3 || pitch < nx || pitch % 4) return fail(FDTD_ERR_INVALID, "bad grid shape");
+  cudaError_t e = prepare_medium_launch(c, ny, nx, pitch, dt, dx, dy, coef, mur, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "prepare_medium");
+  return FDTD_OK;
+}
+
+int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, const float* u,
+                  float* u_next, int32_t src_per_shot, const int32_t* src_row,
+                  const int32_t* src_col, const float* src_w, const int32_t* src_wave,
+                  const float* waveforms, int32_t waveform_len, int32_t step, const float* dense,
+                  int32_t adjoint, void* stream) {
+  if (!grid) return fail(FDTD_ERR_INVALID, "null grid");
+  if (grid->ny < 3 || grid->nx < 3 || grid->pitch < grid->nx || grid->pitch % 4)
+    return fail(FDTD_ERR_INVALID, "bad grid shape");
+  if (!grid->coef || !grid->mur || !u_old || !u || !u_next) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (u_next == u || u_next == u_old) return fail(FDTD_ERR_INVALID, "u_next must not alias the inputs");
+  if (n_shots < 1) return fail(FDTD_ERR_INVALID, "n_shots must be positive");
+  if (src_per_shot > 0 && (!src_row || !src_col || !src_w || !src_wave || !waveforms))
+    return fail(FDTD_ERR_INVALID, "source arrays missing");
+  StepArgs a;
+  a.ny = grid->ny;
+  a.nx = grid->nx;
+  a.pitch = grid->pitch;
+  const double idx2 = 1.0 / (grid->dx * grid->dx), idy2 = 1.0 / (grid->dy * grid->dy);
+  a.idx2 = (float)idx2;
+  a.idy2 = (float)idy2;
+  a.cdiag = (float)(-2.0 * (idx2 + idy2));
+  a.coef = grid->coef;
+  a.mur = grid->mur;
+  a.n_shots = n_shots;
+  a.u_old = u_old;
+  a.u = u;
+  a.u_next = u_next;
+  a.src_per_shot = src_per_shot > 0 ? src_per_shot : 0;
+  a.src_row = src_row;
+  a.src_col = src_col;
+  a.src_w = src_w;
+  a.src_wave = src_wave;
+  a.waveforms = waveforms;
+  a.wave_len = waveform_len;
+  a.step = step;
+  a.dense = dense;
+  a.adjoint = adjoint ? 1 : 0;
+  cudaError_t e = step_launch(a, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "step");
+  return FDTD_OK;
+}
+
+int32_t fdtd_gather(const fdtd_grid* grid, int32_t n_shots, const float* fields, int32_t n_rx,
+                    const int32_t* rx_rc, const float* rx_w, float* out, int64_t out_shot_stride,
+                    int64_t out_rx_stride, void* stream) {
+  if (!grid || !fields || !rx_rc || !rx_w || !out) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (n_shots < 1 || n_rx < 0) return fail(FDTD_ERR_INVALID, "bad sizes");
+  if (n_rx == 0) return FDTD_OK;
+  cudaError_t e = gather_launch(grid->ny, grid->pitch, n_shots, fields, n_rx, rx_rc, rx_w, out,
+                                out_shot_stride, out_rx_stride, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "gather");
+  return FDTD_OK;
+}
+
+int32_t fdtd_scatter(const fdtd_grid* grid, int32_t n_shots, int32_t n_nodes,
+                     const int32_t* tap_nodes, const float* tap_w, const float* residual,
+                     int64_t res_shot_stride, int64_t res_rx_stride, float* dense, void* stream) {
+  if (!grid || !tap_nodes || !tap_w || !residual || !dense) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (n_shots < 1 || n_nodes < 0) return fail(FDTD_ERR_INVALID, "bad sizes");
+  if (n_nodes == 0) return FDTD_OK;
+  cudaError_t e = scatter_launch(grid->ny, grid->pitch, n_shots, n_nodes, tap_nodes, tap_w, residual,
+                                 res_shot_stride, res_rx_stride, dense, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "scatter");
+  return FDTD_OK;
+}
+
+int32_t fdtd_image(const fdtd_grid* grid, int32_t n_shots, const float* adj, const float* fwd,
+                   double scale, double* g, void* stream) {
+  if (!grid || !adj || !fwd || !g) return fail(FDTD_ERR_INVALID, "null pointer");
+  const double idx2 = 1.0 / (grid->dx * grid->dx), idy2 = 1.0 / (grid->dy * grid->dy);
+  cudaError_t e = image_launch(grid->ny, grid->nx, grid->pitch, (float)idx2, (float)idy2,
+                               (float)(-2.0 * (idx2 + idy2)), n_shots, adj, fwd, scale, g,
+                               (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "image");
+  return FDTD_OK;
+}
+
+int32_t fdtd_residual_misfit(int32_t n_shots, int32_t n_rx, int32_t n_steps, const float* traces,
+                             const float* observed, int64_t observed_shot_stride,
+                             const int32_t* mute, float* residual, double* misfit, void* stream) {
+  if (!traces || !observed || !residual || !misfit) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (n_shots < 1 || n_rx < 1 || n_steps < 1) return fail(FDTD_ERR_INVALID, "bad sizes");
+  cudaError_t e = residual_launch(n_shots, n_rx, n_steps, traces, observed, observed_shot_stride,
+                                  mute, residual, misfit, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "residual");
+  return FDTD_OK;
+}
+
+int32_t fdtd_chain_rule(int64_t n, const double* grad_c2, const double* m, const uint8_t* mask,
+                        double* g_m, void* stream) {
+  if (!grad_c2 || !m || !g_m) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (n < 0) return fail(FDTD_ERR_INVALID, "bad size");
+  if (n == 0) return FDTD_OK;
+  cudaError_t e = chain_rule_launch(n, grad_c2, m, mask, g_m, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "chain rule");
+  return FDTD_OK;
+}
+
+// ----------------------------------------------------------------- plans
+
+int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
+                         int32_t for_gradient, fdtd_plan** out) {
+  if (!problem || !out) return fail(FDTD_ERR_INVALID, "null argument");
+  *out = nullptr;
+  int32_t rc = validate_grid(problem->grid);
+  if (rc) return rc;
+  if (problem->n_shots < 1 || problem->n_steps < 1) return fail(FDTD_ERR_INVALID, "n_shots and n_steps must be positive");
+  if (problem->rx.n < 1 || !problem->rx.row0 || !problem->rx.col0 || !problem->rx.w)
+    return fail(FDTD_ERR_INVALID, "receivers missing");
+  if (problem->src.per_shot < 0 || (problem->src.per_shot > 0 &&
+      (!problem->src.row || !problem->src.col || !problem->src.w || !problem->src.wave || !problem->src.waveforms)))
+    return fail(FDTD_ERR_INVALID, "source arrays missing");
+  fdtd_plan* p = new fdtd_plan();
+  p->prob = *problem;
+  fdtd_tuning t;
+  std::memset(&t, 0, sizeof(t));
+  if (tuning) t = *tuning;
+  if (t.rows_per_lane == 0) t.rows_per_lane = 8;
+  if (t.rows_per_lane != 4 && t.rows_per_lane != 8) { delete p; return fail(FDTD_ERR_UNSUPPORTED, "rows_per_lane must be 4 or 8"); }
+  const int max_warps = (t.rows_per_lane == 8) ? 16 : 32;
+  if (t.warps == 0) t.warps = (t.rows_per_lane == 8) ? 16 : 32;
+  if (t.warps < 2 || t.warps > max_warps) { delete p; return fail(FDTD_ERR_UNSUPPORTED, "warps out of range"); }
+  if (t.steps_per_launch == 0) t.steps_per_launch = 12;
+  if (t.steps_per_launch < 1 || t.steps_per_launch > 48) { delete p; return fail(FDTD_ERR_UNSUPPORTED, "steps_per_launch must be in [1, 48]"); }
+  if (t.ctas_per_sm == 0) t.ctas_per_sm = 1;
+  if (t.ckpt_store < 0 || t.ckpt_store > 2) { delete p; return fail(FDTD_ERR_INVALID, "bad checkpoint storage type"); }
+  p->ky = t.rows_per_lane;
+  p->nw = t.warps;
+  p->RY = p->ky * p->nw;
+  p->tmax = t.steps_per_launch;
+  p->for_gradient = for_gradient ? 1 : 0;
+  const int nt = problem->n_steps;
+  if (t.ckpt_every <= 0) {
+    const int c = (int)std::ceil(std::sqrt(2.0 * nt));
+    t.ckpt_every = ((c + p->tmax - 1) / p->tmax) * p->tmax;
+  }
+  if (t.ckpt_every % p->tmax) { delete p; return fail(FDTD_ERR_INVALID, "ckpt_every must be a multiple of steps_per_launch"); }
+  p->ckpt_every = t.ckpt_every;
+  p->nseg = (nt + p->ckpt_every - 1) / p->ckpt_every;
+  p->tun = t;
+  rc = build_tables(p, problem);
+  if (rc) { delete p; return rc; }
+  for (int m = 0; m < 3; ++m) {
+    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->ntap_max, p->nrxl_max, p->tmax).total;
+    if (p->smem[m] > SMEM_LIMIT && (m == MODE_FWD || for_gradient)) {
+      delete p;
+      return fail(FDTD_ERR_UNSUPPORTED, "shared memory need exceeds 227 KB; use fewer steps per launch or warps");
+    }
+  }
+  // workspace layout
+  const fdtd_grid& g = problem->grid;
+  p->field_elems = (size_t)problem->n_shots * g.ny * g.pitch;
+  const size_t fb = p->field_elems * sizeof(float);
+  size_t off = 0;
+  p->o_tiles = off; off = align_up(off + p->tiles.size() * sizeof(TbTile));
+  p->o_taps = off; off = align_up(off + std::max<size_t>(1, p->taps.size()) * sizeof(TbTap));
+  p->o_rxl = off; off = align_up(off + std::max<size_t>(1, p->rxl.size()) * sizeof(int));
+  p->o_recs = off; off = align_up(off + std::max<size_t>(1, p->recs.size()) * sizeof(TbRec));
+  p->o_src = off; off = align_up(off + p->src.size() * sizeof(SrcNode));
+  p->o_nsrc = off; off = align_up(off + p->nsrc.size() * sizeof(int));
+  for (int s = 0; s < 2; ++s)
+    for (int f = 0; f < 2; ++f) { p->o_state[s][f] = off; off = align_up(off + fb); }
+  if (p->for_gradient) {
+    for (int s = 0; s < 2; ++s)
+      for (int f = 0; f < 2; ++f) { p->o_adj[s][f] = off; off = align_up(off + fb); }
+    p->ckpt_elem_bytes = (t.ckpt_store == FDTD_STORE_F32) ? 4 : 2;
+    const size_t nck = (size_t)(p->nseg - 1) * 2;  // checkpoints 1..nseg-1, two fields each
+    p->o_ckpt = off; off = align_up(off + nck * p->field_elems * p->ckpt_elem_bytes);
+    p->o_scales = off; off = align_up(off + nck * 2 * problem->n_shots * sizeof(float) + 16);
+    p->o_seg = off; off = align_up(off + (size_t)p->ckpt_every * fb);
+  }
+  p->total = off;
+  *out = p;
+  return FDTD_OK;
+}
+
+int32_t fdtd_plan_destroy(fdtd_plan* plan) {
+  delete plan;
+  return FDTD_OK;
+}
+
+int32_t fdtd_plan_workspace_bytes(const fdtd_plan* plan, size_t* bytes) {
+  if (!plan || !bytes) return fail(FDTD_ERR_INVALID, "null argument");
+  *bytes = plan->total;
+  return FDTD_OK;
+}
+
+int32_t fdtd_plan_tuning(const fdtd_plan* plan, fdtd_tuning* tuning) {
+  if (!plan || !tuning) return fail(FDTD_ERR_INVALID, "null argument");
+  *tuning = plan->tun;
+  return FDTD_OK;
+}
+
+int32_t fdtd_plan_bind(fdtd_plan* p, void* workspace, size_t bytes, void* stream) {
+  if (!p || !workspace) return fail(FDTD_ERR_WORKSPACE, "workspace missing");
+  if (bytes < p->total) return fail(FDTD_ERR_WORKSPACE, "workspace too small: need " + std::to_string(p->total) + " bytes");
+  if (reinterpret_cast<uintptr_t>(workspace) % ALIGN) return fail(FDTD_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+  p->ws = reinterpret_cast<char*>(workspace);
+  p->ws_bytes = bytes;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  struct Up { size_t off; const void* src; size_t n; };
+  const Up ups[] = {
+      {p->o_tiles, p->tiles.data(), p->tiles.size() * sizeof(TbTile)},
+      {p->o_taps, p->taps.data(), p->taps.size() * sizeof(TbTap)},
+      {p->o_rxl, p->rxl.data(), p->rxl.size() * sizeof(int)},
+      {p->o_recs, p->recs.data(), p->recs.size() * sizeof(TbRec)},
+      {p->o_src, p->src.data(), p->src.size() * sizeof(SrcNode)},
+      {p->o_nsrc, p->nsrc.data(), p->nsrc.size() * sizeof(int)},
+  };
+  for (const Up& u : ups) {
+    if (!u.n) continue;
+    e = cudaMemcpyAsync(p->ws + u.off, u.src, u.n, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "table upload");
+  }
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "table upload sync");
+  p->bound = true;
+  p->have_ckpt = false;
+  return FDTD_OK;
+}
+
+int32_t fdtd_plan_set_medium(fdtd_plan* p, const float* coef, const float* mur, const float* waveforms) {
+  if (!p) return fail(FDTD_ERR_INVALID, "null plan");
+  if (coef) p->prob.grid.coef = coef;
+  if (mur) p->prob.grid.mur = mur;
+  if (waveforms) p->prob.src.waveforms = waveforms;
+  p->have_ckpt = false;
+  return FDTD_OK;
+}
+
+int32_t fdtd_forward(fdtd_plan* p, float* traces, float* u_prev_out, float* u_out,
+                     int32_t save_checkpoints, void* stream) {
+  if (!p || !p->bound) return fail(FDTD_ERR_STATE, "plan is not bound to a workspace");
+  if (!traces) return fail(FDTD_ERR_INVALID, "traces must be set");
+  if ((u_prev_out == nullptr) != (u_out == nullptr)) return fail(FDTD_ERR_INVALID, "give both final-state outputs or neither");
+  if (save_checkpoints && !p->for_gradient) return fail(FDTD_ERR_STATE, "plan was created without gradient storage");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t fb = p->field_elems * sizeof(float);
+  cudaError_t e = cudaMemsetAsync(p->ws + p->o_state[0][0], 0, fb, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->ws + p->o_state[0][1], 0, fb, st);
+  if (e != cudaSuccess) return cuda_fail(e, "state reset");
+  TbParams q;
+  fill_params(p, q);
+  q.traces = traces;
+  const int nt = p->prob.n_steps, T = p->tmax, C = p->ckpt_every;
+  const float* in_prev = fptr(p, p->o_state[0][0]);
+  const float* in_cur = fptr(p, p->o_state[0][1]);
+  int in_set = 0;  // 0/1 = ping-pong set, -1 = elsewhere
+  for (int n0 = 0; n0 < nt; n0 += T) {
+    const int ns = std::min(T, nt - n0), end = n0 + ns;
+    const int out_set = (in_set == 0) ? 1 : 0;
+    float* out_prev = fptr(p, p->o_state[out_set][0]);
+    float* out_cur = fptr(p, p->o_state[out_set][1]);
+    int next_set = out_set;
+    const bool ckpt = save_checkpoints && end < nt && end % C == 0;
+    const int j = end / C;
+    if (end == nt && u_out) {
+      out_prev = u_prev_out;
+      out_cur = u_out;
+      next_set = -1;
+    } else if (ckpt && p->tun.ckpt_store == FDTD_STORE_F32) {
+      const size_t base = p->o_ckpt + (size_t)(j - 1) * 2 * fb;
+      out_prev = fptr(p, base);
+      out_cur = fptr(p, base + fb);
+      next_set = -1;
+    }
+    q.in_prev = in_prev;
+    q.in_cur = in_cur;
+    q.out_prev = out_prev;
+    q.out_cur = out_cur;
+    q.n0 = n0;
+    q.nsteps = ns;
+    int32_t rc = launch(p, q, MODE_FWD, st);
+    if (rc) return rc;
+    if (ckpt && p->tun.ckpt_store != FDTD_STORE_F32) {
+      const size_t eb = p->field_elems * p->ckpt_elem_bytes;
+      const long long per_shot = (long long)p->prob.grid.ny * p->prob.grid.pitch;
+      for (int f = 0; f < 2; ++f) {
+        char* dst = p->ws + p->o_ckpt + ((size_t)(j - 1) * 2 + f) * eb;
+        float* sc = fptr(p, p->o_scales) + ((size_t)(j - 1) * 2 + f) * 2 * p->prob.n_shots;
+        e = quantize_launch(f == 0 ? out_prev : out_cur, dst, sc, p->prob.n_shots, per_shot, p->tun.ckpt_store, st);
+        if (e != cudaSuccess) return cuda_fail(e, "checkpoint quantise");
+      }
+    }
+    in_prev = out_prev;
+    in_cur = out_cur;
+    in_set = next_set;
+  }
+  p->have_ckpt = save_checkpoints != 0;
+  return FDTD_OK;
+}
+
+int32_t fdtd_adjoint(fdtd_plan* p, const float* residual, double* grad_c2, void* stream) {
+  if (!p || !p->bound) return fail(FDTD_ERR_STATE, "plan is not bound to a workspace");
+  if (!p->have_ckpt) return fail(FDTD_ERR_STATE, "run fdtd_forward with save_checkpoints first");
+  if (!residual || !grad_c2) return fail(FDTD_ERR_INVALID, "null pointer");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t fb = p->field_elems * sizeof(float);
+  cudaError_t e = cudaMemsetAsync(p->ws + p->o_adj[0][0], 0, fb, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->ws + p->o_adj[0][1], 0, fb, st);
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint reset");
+  TbParams q;
+  fill_params(p, q);
+  q.residual = residual;
+  q.grad = grad_c2;
+  q.scale = p->prob.grid.dt * p->prob.grid.dt;
+  q.seg = fptr(p, p->o_seg);
+  const int nt = p->prob.n_steps, T = p->tmax, C = p->ckpt_every;
+  int adj_in = 0;
+  const long long per_shot = (long long)p->prob.grid.ny * p->prob.grid.pitch;
+  for (int j = p->nseg - 1; j >= 0; --j) {
+    const int a = j * C, b = std::min(a + C, nt);
+    const float* in_prev;
+    const float* in_cur;
+    int in_set;
+    if (j == 0) {
+      e = cudaMemsetAsync(p->ws + p->o_state[0][0], 0, fb, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(p->ws + p->o_state[0][1], 0, fb, st);
+      if (e != cudaSuccess) return cuda_fail(e, "recompute reset");
+      in_prev = fptr(p, p->o_state[0][0]);
+      in_cur = fptr(p, p->o_state[0][1]);
+      in_set = 0;
+    } else if (p->tun.ckpt_store == FDTD_STORE_F32) {
+      const size_t base = p->o_ckpt + (size_t)(j - 1) * 2 * fb;
+      in_prev = fptr(p, base);
+      in_cur = fptr(p, base + fb);
+      in_set = -1;
+    } else {
+      const size_t eb = p->field_elems * p->ckpt_elem_bytes;
+      for (int f = 0; f < 2; ++f) {
+        const char* src = p->ws + p->o_ckpt + ((size_t)(j - 1) * 2 + f) * eb;
+        const float* sc = fptr(p, p->o_scales) + ((size_t)(j - 1) * 2 + f) * 2 * p->prob.n_shots;
+        e = dequantize_launch(src, sc, fptr(p, p->o_state[0][f]), p->prob.n_shots, per_shot,
+                              p->tun.ckpt_store, st);
+        if (e != cudaSuccess) return cuda_fail(e, "checkpoint dequantise");
+      }
+      in_prev = fptr(p, p->o_state[0][0]);
+      in_cur = fptr(p, p->o_state[0][1]);
+      in_set = 0;
+    }
+    // recompute the segment, keeping lap(u^{n-1}) of every step n in [a, b)
+    q.seg_base = a;
+    for (int n0 = a; n0 < b; n0 += T) {
+      const int ns = std::min(T, b - n0);
+      const int out_set = (in_set == 0) ? 1 : 0;
+      q.in_prev = in_prev;
+      q.in_cur = in_cur;
+      q.out_prev = fptr(p, p->o_state[out_set][0]);
+      q.out_cur = fptr(p, p->o_state[out_set][1]);
+      q.n0 = n0;
+      q.nsteps = ns;
+      int32_t rc = launch(p, q, MODE_REC, st);
+      if (rc) return rc;
+      in_prev = q.out_prev;
+      in_cur = q.out_cur;
+      in_set = out_set;
+    }
+    // reverse-time adjoint over the segment
+    for (int ntop = b - 1; ntop >= a; ntop -= T) {
+      const int ns = std::min(T, ntop - a + 1);
+      const int out = adj_in ^ 1;
+      q.in_prev = fptr(p, p->o_adj[adj_in][0]);
+      q.in_cur = fptr(p, p->o_adj[adj_in][1]);
+      q.out_prev = fptr(p, p->o_adj[out][0]);
+      q.out_cur = fptr(p, p->o_adj[out][1]);
+      q.n0 = ntop;
+      q.nsteps = ns;
+      int32_t rc = launch(p, q, MODE_ADJ, st);
+      if (rc) return rc;
+      adj_in = out;
+    }
+  }
+  return FDTD_OK;
+}
+
+// ----------------------------------------------------------- plain engine
+
+size_t fdtd_forward_plain_workspace(const fdtd_problem* prob) {
+  if (!prob) return 0;
+  const size_t plane = (size_t)prob->grid.ny * prob->grid.pitch * sizeof(float);
+  const size_t R = prob->rx.n;
+  const size_t K = prob->src.per_shot > 0 ? prob->src.per_shot : 0;
+  return align_up(3 * plane) + align_up(R * 2 * sizeof(int32_t)) + align_up(R * 4 * sizeof(float)) +
+         align_up((size_t)prob->n_shots * K * (3 * sizeof(int32_t) + sizeof(float)) + 16);
+}
+
+int32_t fdtd_forward_plain(const fdtd_problem* prob, float* traces, void* workspace, size_t bytes,
+                           void* stream) {
+  if (!prob || !traces) return fail(FDTD_ERR_INVALID, "null argument");
+  int32_t rc = validate_grid(prob->grid);
+  if (rc) return rc;
+  if (!workspace || bytes < fdtd_forward_plain_workspace(prob)) return fail(FDTD_ERR_WORKSPACE, "workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  const fdtd_grid& g = prob->grid;
+  const size_t plane = (size_t)g.ny * g.pitch;
+  const int R = prob->rx.n, S = prob->n_shots, nt = prob->n_steps;
+  const int K = prob->src.per_shot > 0 ? prob->src.per_shot : 0;
+  char* w = reinterpret_cast<char*>(workspace);
+  float* f[3] = {reinterpret_cast<float*>(w), reinterpret_cast<float*>(w) + plane,
+                 reinterpret_cast<float*>(w) + 2 * plane};
+  size_t off = align_up(3 * plane * sizeof(float));
+  int32_t* rx_rc = reinterpret_cast<int32_t*>(w + off);
+  off += align_up((size_t)R * 2 * sizeof(int32_t));
+  float* rx_w = reinterpret_cast<float*>(w + off);
+  off += align_up((size_t)R * 4 * sizeof(float));
+  int32_t* s_row = reinterpret_cast<int32_t*>(w + off);
+  int32_t* s_col = s_row + (size_t)S * K;
+  int32_t* s_wave = s_col + (size_t)S * K;
+  float* s_w = reinterpret_cast<float*>(s_wave + (size_t)S * K);
+  std::vector<int32_t> rc_h(2 * (size_t)R);
+  for (int r = 0; r < R; ++r) { rc_h[2 * r] = prob->rx.row0[r]; rc_h[2 * r + 1] = prob->rx.col0[r]; }
+  cudaError_t e = cudaMemcpyAsync(rx_rc, rc_h.data(), rc_h.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rx_w, prob->rx.w, (size_t)R * 4 * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (K > 0) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_row, prob->src.row, (size_t)S * K * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_col, prob->src.col, (size_t)S * K * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_wave, prob->src.wave, (size_t)S * K * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_w, prob->src.w, (size_t)S * K * 4, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "plain forward upload");
+  for (int s = 0; s < S; ++s) {
+    e = cudaMemsetAsync(w, 0, 3 * plane * sizeof(float), st);
+    if (e != cudaSuccess) return cuda_fail(e, "plain forward reset");
+    int io = 0, ic = 1, in = 2;
+    for (int n = 0; n < nt; ++n) {
+      rc = fdtd_step(&g, 1, f[io], f[ic], f[in], K, s_row + (size_t)s * K, s_col + (size_t)s * K,
+                     s_w + (size_t)s * K, s_wave + (size_t)s * K, prob->src.waveforms,
+                     prob->src.waveform_len, n, nullptr, 0, stream);
+      if (rc) return rc;
+      e = gather_launch(g.ny, g.pitch, 1, f[in], R, rx_rc, rx_w, traces + (size_t)s * R * nt + n, 0, nt, st);
+      if (e != cudaSuccess) return cuda_fail(e, "plain gather");
+      const int t = io; io = ic; ic = in; in = t;
+    }
+  }
+  return FDTD_OK;
+}
+
+}  // extern "C"

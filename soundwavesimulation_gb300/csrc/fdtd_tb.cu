@@ -1,0 +1,565 @@
+// Temporally blocked, shot-batched leapfrog kernel (forward, recompute, adjoint).
+//
+// One CTA works on one (tile, shot) item at a time, persistently. A tile is a
+// region of 128 columns x (warps * KY) rows. Lane `l` of warp `w` keeps, in
+// registers, columns 4l..4l+3 of rows w*KY..w*KY+KY-1 of the two live fields
+// (u_old and u). A launch advances every region by `nsteps` leapfrog steps
+// without touching HBM between steps:
+//   - x-neighbours come from warp shuffles (the warp spans the whole region
+//     width, so no shared memory is needed in x);
+//   - y-neighbours inside a band stay in registers; the first and last row of
+//     every band go through a double-buffered shared-memory exchange, one
+//     __syncthreads per step;
+//   - the region carries a halo of at least nsteps+1 cells at every border that
+//     is not a domain edge, so the cells a tile owns are still exact after the
+//     last step (overlapped temporal blocking); owned cells partition the grid
+//     and are the only ones written back;
+//   - Mur edges and corners (fdtd2d/torch_backend.py:477-490), soft sources
+//     (fdtd2d/torch_backend.py:517), the residual injection
+//     (fdtd2d/torch_backend.py:563-580), the receiver gather
+//     (fdtd2d/torch_backend.py:540-548), the per-step Laplacian of the forward
+//     field (recompute) and the imaging condition
+//     (fdtd2d/torch_backend.py:583-598) are all applied inside the block.
+// The arithmetic helpers in fdtd_device.cuh make every value bit-identical to
+// the one-step kernels in fdtd_kernels.cu.
+
+#include "fdtd_device.cuh"
+#include "fdtd_internal.h"
+
+namespace fdtd {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+struct Ctx {
+  int tid, w, lane, nw, s;
+  int rx0, ry0, flags;
+  int y0, xb;               // global row of this thread's r = 0, column of c = 0
+  unsigned own_rows, own_cols;
+  unsigned mask, srcsel;
+  int base;
+  float* s_coef;
+  float* s_g;
+  float4* s_xch;
+  float* s_tap;
+  const float* s_src;
+  const int* s_srcpos;
+};
+
+template <int MODE>
+__device__ __forceinline__ float4 opval(const float (&v)[4], float4 co) {
+  if (MODE == MODE_ADJ) {
+    return make_float4(__fmul_rn(co.x, v[0]), __fmul_rn(co.y, v[1]), __fmul_rn(co.z, v[2]),
+                       __fmul_rn(co.w, v[3]));
+  }
+  return make_float4(v[0], v[1], v[2], v[3]);
+}
+
+__device__ __forceinline__ float4 ldg4(const float* p) {
+  return __ldg(reinterpret_cast<const float4*>(p));
+}
+
+template <int KY, int MODE, bool EDGE>
+__device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
+                                        const TbParams& p, const Ctx& x, int k) {
+  const int n = (MODE == MODE_ADJ) ? p.n0 - k : p.n0 + k;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4* xin = x.s_xch + (k & 1) * x.nw * 64;
+  float4* xout = x.s_xch + ((k + 1) & 1) * x.nw * 64;
+  const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
+  const float idx2 = p.idx2, idy2 = p.idy2, cdiag = p.cdiag;
+
+  // ---- stencil over the band, rolling the row above / below
+  float4 prv = (x.w > 0) ? xin[(x.w - 1) * 64 + 32 + x.lane] : zero4;
+  const float4 below = (x.w < x.nw - 1) ? xin[(x.w + 1) * 64 + x.lane] : zero4;
+  float4 cur = opval<MODE>(C[0], coef4[0]);
+  const bool lzero = EDGE && x.lane == 0 && x.rx0 == 0;
+  const bool rzero = EDGE && x.lane == 31 && (x.rx0 + RX >= p.nx);
+  float* segrow = nullptr;
+  if (MODE == MODE_REC) {
+    segrow = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
+             ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
+  }
+#pragma unroll
+  for (int r = 0; r < KY; ++r) {
+    const float4 nxt = (r + 1 < KY) ? opval<MODE>(C[r + 1], coef4[(r + 1) * 32]) : below;
+    float lft = __shfl_up_sync(FULL, cur.w, 1);
+    float rgt = __shfl_down_sync(FULL, cur.x, 1);
+    if (lzero) lft = 0.f;
+    if (rzero) rgt = 0.f;
+    const float l0 = lap5(cur.x, lft, cur.y, prv.x, nxt.x, idx2, idy2, cdiag);
+    const float l1 = lap5(cur.y, cur.x, cur.z, prv.y, nxt.y, idx2, idy2, cdiag);
+    const float l2 = lap5(cur.z, cur.y, cur.w, prv.z, nxt.z, idx2, idy2, cdiag);
+    const float l3 = lap5(cur.w, cur.z, rgt, prv.w, nxt.w, idx2, idy2, cdiag);
+    if (MODE == MODE_ADJ) {
+      P[r][0] = leap_adj(C[r][0], P[r][0], l0);
+      P[r][1] = leap_adj(C[r][1], P[r][1], l1);
+      P[r][2] = leap_adj(C[r][2], P[r][2], l2);
+      P[r][3] = leap_adj(C[r][3], P[r][3], l3);
+    } else {
+      const float4 co = coef4[r * 32];
+      P[r][0] = leap(C[r][0], P[r][0], co.x, l0);
+      P[r][1] = leap(C[r][1], P[r][1], co.y, l1);
+      P[r][2] = leap(C[r][2], P[r][2], co.z, l2);
+      P[r][3] = leap(C[r][3], P[r][3], co.w, l3);
+    }
+    if (MODE == MODE_REC && ((x.own_rows >> r) & 1u)) {
+      float* dst = segrow + (long long)r * p.pitch;
+      if (x.own_cols == 0xFu) {
+        *reinterpret_cast<float4*>(dst) = make_float4(l0, l1, l2, l3);
+      } else {
+        if (x.own_cols & 1u) dst[0] = l0;
+        if (x.own_cols & 2u) dst[1] = l1;
+        if (x.own_cols & 4u) dst[2] = l2;
+        if (x.own_cols & 8u) dst[3] = l3;
+      }
+    }
+    prv = cur;
+    cur = nxt;
+  }
+
+  // ---- injection before the boundary update
+  if (MODE != MODE_ADJ) {
+    unsigned sel = x.srcsel;
+    while (sel) {
+      const int j = __ffs(sel) - 1;
+      sel &= sel - 1u;
+      const int bit = x.s_srcpos[j] & 255;
+      const float v = x.s_src[k * SRC_MAX + j];
+#pragma unroll
+      for (int b = 0; b < 4 * KY; ++b) {
+        if (b == bit) P[b >> 2][b & 3] = inj_add(P[b >> 2][b & 3], v);
+      }
+    }
+  } else if (x.mask) {
+    int slot = x.base;
+    const float* inj = x.s_tap + k * p.ntap_max;
+#pragma unroll
+    for (int b = 0; b < 4 * KY; ++b) {
+      if ((x.mask >> b) & 1u) {
+        P[b >> 2][b & 3] = inj_add(P[b >> 2][b & 3], inj[slot]);
+        ++slot;
+      }
+    }
+  }
+
+  // ---- Mur edges and corners, zero outside the domain
+  if (EDGE) {
+    const int nx = p.nx, ny = p.ny;
+    const float* kl = p.mur;
+    const float* kr = kl + ny;
+    const float* kb = kr + ny;
+    const float* kt = kb + nx;
+    const float* ckx = kt + nx;
+    const float* cky = ckx + 4;
+    const int rb = -x.y0;            // local row of global row 0
+    const int rt = ny - 1 - x.y0;    // local row of global row ny-1
+    if (x.flags & TF_BOTTOM) {
+#pragma unroll
+      for (int r = 0; r + 1 < KY; ++r) {
+        if (r == rb) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int xx = x.xb + c;
+            if (xx >= 1 && xx <= nx - 2) P[r][c] = mur(C[r + 1][c], __ldg(kb + xx), P[r + 1][c], C[r][c]);
+          }
+        }
+      }
+    }
+    if (x.flags & TF_TOP) {
+#pragma unroll
+      for (int r = 1; r < KY; ++r) {
+        if (r == rt) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int xx = x.xb + c;
+            if (xx >= 1 && xx <= nx - 2) P[r][c] = mur(C[r - 1][c], __ldg(kt + xx), P[r - 1][c], C[r][c]);
+          }
+        }
+      }
+    }
+    if ((x.flags & TF_LEFT) && x.lane == 0) {  // the tiler puts column 0 at lane 0, c = 0
+#pragma unroll
+      for (int r = 0; r < KY; ++r) {
+        const int yy = x.y0 + r;
+        if (yy >= 1 && yy <= ny - 2) P[r][0] = mur(C[r][1], __ldg(kl + yy), P[r][1], C[r][0]);
+      }
+    }
+    if (x.flags & TF_RIGHT) {
+      const int lx1 = nx - 1 - x.rx0;
+      const int L1 = lx1 >> 2, c1 = lx1 & 3;
+      // Values of column nx-2 at this lane's rows: same lane (c1 >= 1) or the
+      // previous lane's column 3 (c1 == 0). Taken after the row-0/ny-1 updates so
+      // the corners below see the updated edge values.
+      float su[KY], sn[KY];
+#pragma unroll
+      for (int r = 0; r < KY; ++r) {
+        su[r] = __shfl_up_sync(FULL, C[r][3], 1);
+        sn[r] = __shfl_up_sync(FULL, P[r][3], 1);
+      }
+      if (x.lane == L1) {
+#pragma unroll
+        for (int r = 0; r < KY; ++r) {
+          const int yy = x.y0 + r;
+          if (yy >= 1 && yy <= ny - 2) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (c == c1) {
+                const float uin = (c == 0) ? su[r] : C[r][c > 0 ? c - 1 : 0];
+                const float nin = (c == 0) ? sn[r] : P[r][c > 0 ? c - 1 : 0];
+                P[r][c] = mur(uin, __ldg(kr + yy), nin, C[r][c]);
+              }
+            }
+          }
+        }
+        // corners (0, nx-1) and (ny-1, nx-1)
+#pragma unroll
+        for (int r = 0; r < KY; ++r) {
+          const bool bot = (x.flags & TF_BOTTOM) && r == rb && r + 1 < KY;
+          const bool top = (x.flags & TF_TOP) && r == rt && r >= 1;
+          if (bot || top) {
+            const int rn = bot ? (r + 1 < KY ? r + 1 : r) : (r >= 1 ? r - 1 : r);
+            const int ci = bot ? 1 : 3;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (c == c1) {
+                const float uin = (c == 0) ? su[r] : C[r][c > 0 ? c - 1 : 0];
+                const float nin = (c == 0) ? sn[r] : P[r][c > 0 ? c - 1 : 0];
+                const float fx = mur(uin, __ldg(ckx + ci), nin, C[r][c]);
+                const float fy = mur(C[rn][c], __ldg(cky + ci), P[rn][c], C[r][c]);
+                P[r][c] = corner_avg(fx, fy);
+              }
+            }
+          }
+        }
+      }
+    }
+    if ((x.flags & TF_LEFT) && x.lane == 0) {  // corners (0, 0) and (ny-1, 0)
+#pragma unroll
+      for (int r = 0; r < KY; ++r) {
+        const bool bot = (x.flags & TF_BOTTOM) && r == rb && r + 1 < KY;
+        const bool top = (x.flags & TF_TOP) && r == rt && r >= 1;
+        if (bot || top) {
+          const int rn = bot ? (r + 1 < KY ? r + 1 : r) : (r >= 1 ? r - 1 : r);
+          const int ci = bot ? 0 : 2;
+          const float fx = mur(C[r][1], __ldg(ckx + ci), P[r][1], C[r][0]);
+          const float fy = mur(C[rn][0], __ldg(cky + ci), P[rn][0], C[r][0]);
+          P[r][0] = corner_avg(fx, fy);
+        }
+      }
+    }
+    if (x.flags & TF_OUTSIDE) {
+#pragma unroll
+      for (int r = 0; r < KY; ++r) {
+        const int yy = x.y0 + r;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (yy < 0 || yy >= ny || x.xb + c >= nx) P[r][c] = 0.f;
+        }
+      }
+    }
+  }
+
+  // ---- receiver taps (forward) / imaging (adjoint)
+  if (MODE == MODE_FWD && x.mask) {
+    int slot = x.base;
+    float* rec = x.s_tap + k * p.ntap_max;
+#pragma unroll
+    for (int b = 0; b < 4 * KY; ++b) {
+      if ((x.mask >> b) & 1u) {
+        rec[slot] = P[b >> 2][b & 3];
+        ++slot;
+      }
+    }
+  }
+  if (MODE == MODE_ADJ && n >= 1) {
+    const float* sl = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
+                      ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
+    float4* g4 = reinterpret_cast<float4*>(x.s_g) + (x.w * KY) * 32 + x.lane;
+#pragma unroll
+    for (int r = 0; r < KY; ++r) {
+      if ((x.own_rows >> r) & 1u) {
+        float4 lv;
+        if (x.own_cols == 0xFu) {
+          lv = ldg4(sl + (long long)r * p.pitch);
+        } else {
+          const float* q = sl + (long long)r * p.pitch;
+          lv.x = (x.own_cols & 1u) ? __ldg(q + 0) : 0.f;
+          lv.y = (x.own_cols & 2u) ? __ldg(q + 1) : 0.f;
+          lv.z = (x.own_cols & 4u) ? __ldg(q + 2) : 0.f;
+          lv.w = (x.own_cols & 8u) ? __ldg(q + 3) : 0.f;
+        }
+        float4 gv = g4[r * 32];
+        if (x.own_cols & 1u) gv.x = __fmaf_rn(P[r][0], lv.x, gv.x);
+        if (x.own_cols & 2u) gv.y = __fmaf_rn(P[r][1], lv.y, gv.y);
+        if (x.own_cols & 4u) gv.z = __fmaf_rn(P[r][2], lv.z, gv.z);
+        if (x.own_cols & 8u) gv.w = __fmaf_rn(P[r][3], lv.w, gv.w);
+        g4[r * 32] = gv;
+      }
+    }
+  }
+
+  // ---- publish the band's first and last rows for the next step
+  xout[x.w * 64 + x.lane] = opval<MODE>(P[0], coef4[0]);
+  xout[x.w * 64 + 32 + x.lane] = opval<MODE>(P[KY - 1], coef4[(KY - 1) * 32]);
+  __syncthreads();
+}
+
+template <int KY>
+__device__ __forceinline__ void store_state(const TbParams& p, const Ctx& x,
+                                            const float (&prev)[KY][4], const float (&cur)[KY][4]) {
+  const long long base = ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
+#pragma unroll
+  for (int r = 0; r < KY; ++r) {
+    if ((x.own_rows >> r) & 1u) {
+      float* dp = p.out_prev + base + (long long)r * p.pitch;
+      float* dc = p.out_cur + base + (long long)r * p.pitch;
+      if (x.own_cols == 0xFu) {
+        *reinterpret_cast<float4*>(dp) = make_float4(prev[r][0], prev[r][1], prev[r][2], prev[r][3]);
+        *reinterpret_cast<float4*>(dc) = make_float4(cur[r][0], cur[r][1], cur[r][2], cur[r][3]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if ((x.own_cols >> c) & 1u) {
+            dp[c] = prev[r][c];
+            dc[c] = cur[r][c];
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int KY, int MODE, bool EDGE>
+__device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
+  float P[KY][4], C[KY][4];
+  const long long sbase = (long long)x.s * p.ny * p.pitch;
+#pragma unroll
+  for (int r = 0; r < KY; ++r) {
+    const int yy = x.y0 + r;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    if (yy >= 0 && yy < p.ny && x.xb < p.pitch) {
+      a = ldg4(p.in_prev + sbase + (long long)yy * p.pitch + x.xb);
+      b = ldg4(p.in_cur + sbase + (long long)yy * p.pitch + x.xb);
+    }
+    P[r][0] = a.x; P[r][1] = a.y; P[r][2] = a.z; P[r][3] = a.w;
+    C[r][0] = b.x; C[r][1] = b.y; C[r][2] = b.z; C[r][3] = b.w;
+    if (EDGE) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (x.xb + c >= p.nx) { P[r][c] = 0.f; C[r][c] = 0.f; }
+      }
+    }
+  }
+  const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
+  x.s_xch[x.w * 64 + x.lane] = opval<MODE>(C[0], coef4[0]);
+  x.s_xch[x.w * 64 + 32 + x.lane] = opval<MODE>(C[KY - 1], coef4[(KY - 1) * 32]);
+  __syncthreads();
+
+  for (int k = 0; k < p.nsteps; k += 2) {
+    substep<KY, MODE, EDGE>(P, C, p, x, k);
+    if (k + 1 < p.nsteps) substep<KY, MODE, EDGE>(C, P, p, x, k + 1);
+  }
+  if (p.nsteps & 1) {
+    store_state<KY>(p, x, C, P);
+  } else {
+    store_state<KY>(p, x, P, C);
+  }
+}
+
+template <int KY, int MODE>
+__global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbParams p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nw = p.nwarps;
+  const int nthr = nw * 32;
+  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.ntap_max, p.nrxl_max, p.tmax);
+  Ctx x;
+  x.tid = threadIdx.x;
+  x.w = x.tid >> 5;
+  x.lane = x.tid & 31;
+  x.nw = nw;
+  x.s_coef = reinterpret_cast<float*>(smem + L.coef);
+  x.s_g = reinterpret_cast<float*>(smem + L.g);
+  x.s_xch = reinterpret_cast<float4*>(smem + L.xch);
+  x.s_tap = reinterpret_cast<float*>(smem + L.tap);
+  float* s_res = reinterpret_cast<float*>(smem + L.res);
+  float* s_src = reinterpret_cast<float*>(smem + L.src);
+  unsigned* s_mask = reinterpret_cast<unsigned*>(smem + L.mask);
+  int* s_base = reinterpret_cast<int*>(smem + L.base);
+  int* s_srcpos = reinterpret_cast<int*>(smem + L.srcpos);
+  x.s_src = s_src;
+  x.s_srcpos = s_srcpos;
+  const int RY = nw * KY;
+  const int nitems = p.ntiles * p.nshots;
+
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int ti = item / p.nshots;
+    const int s = item - ti * p.nshots;
+    const TbTile t = p.tiles[ti];
+    x.s = s;
+    x.rx0 = t.rx0;
+    x.ry0 = t.ry0;
+    x.flags = t.flags;
+    x.y0 = t.ry0 + x.w * KY;
+    x.xb = t.rx0 + 4 * x.lane;
+    x.own_rows = 0;
+#pragma unroll
+    for (int r = 0; r < KY; ++r) {
+      const int yy = x.y0 + r;
+      if (yy >= t.oy0 && yy < t.oy1) x.own_rows |= 1u << r;
+    }
+    x.own_cols = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int xx = x.xb + c;
+      if (xx >= t.ox0 && xx < t.ox1) x.own_cols |= 1u << c;
+    }
+
+    // coefficients of the region (zero outside the domain)
+#pragma unroll
+    for (int r = 0; r < KY; ++r) {
+      const int yy = x.y0 + r;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (yy >= 0 && yy < p.ny && x.xb < p.pitch) v = ldg4(p.coef + (long long)yy * p.pitch + x.xb);
+      if (x.xb + 0 >= p.nx) v.x = 0.f;
+      if (x.xb + 1 >= p.nx) v.y = 0.f;
+      if (x.xb + 2 >= p.nx) v.z = 0.f;
+      if (x.xb + 3 >= p.nx) v.w = 0.f;
+      reinterpret_cast<float4*>(x.s_coef)[(x.w * KY + r) * 32 + x.lane] = v;
+      if (MODE == MODE_ADJ) {
+        reinterpret_cast<float4*>(x.s_g)[(x.w * KY + r) * 32 + x.lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    s_mask[x.tid] = 0u;
+    s_base[x.tid] = 0x7fffffff;
+    if (x.tid < SRC_MAX) {
+      int pos = -1;
+      if (MODE != MODE_ADJ && x.tid < p.nsrc[s]) {
+        const SrcNode sn = p.src[s * SRC_MAX + x.tid];
+        const int ly = sn.row - t.ry0, lx = sn.col - t.rx0;
+        if (ly >= 0 && ly < RY && lx >= 0 && lx < RX) {
+          pos = (((ly / KY) * 32 + (lx >> 2)) << 8) | ((ly % KY) * 4 + (lx & 3));
+        }
+      }
+      s_srcpos[x.tid] = pos;
+    }
+    if (MODE != MODE_ADJ) {
+      for (int i = x.tid; i < p.nsteps * SRC_MAX; i += nthr) {
+        const int k = i / SRC_MAX, j = i - k * SRC_MAX;
+        float acc = 0.f;
+        if (j < p.nsrc[s]) {
+          const SrcNode sn = p.src[s * SRC_MAX + j];
+          const int nstep = p.n0 + k;
+#pragma unroll
+          for (int q = 0; q < SRC_C; ++q) {
+            if (sn.wave[q] >= 0) {
+              const float v = (nstep < p.wave_len) ? __ldg(p.waveforms + (long long)sn.wave[q] * p.wave_len + nstep) : 0.f;
+              acc = inj_acc(acc, sn.w[q], v);
+            }
+          }
+        }
+        s_src[i] = acc;
+      }
+    } else {
+      for (int i = x.tid; i < t.nrxl * p.nsteps; i += nthr) {
+        const int j = i / p.nsteps, k = i - j * p.nsteps;
+        const int rg = __ldg(p.rxl + t.rxl_off + j);
+        s_res[j * p.tmax + k] = __ldg(p.residual + ((long long)s * p.nrx + rg) * p.nt + (p.n0 - k));
+      }
+    }
+    __syncthreads();
+    for (int i = x.tid; i < t.ntap; i += nthr) {
+      const int pk = p.taps[t.tap_off + i].packed;
+      atomicOr(&s_mask[pk >> 8], 1u << (pk & 255));
+      atomicMin(&s_base[pk >> 8], i);
+    }
+    __syncthreads();
+    if (MODE == MODE_ADJ) {
+      for (int i = x.tid; i < t.ntap * p.nsteps; i += nthr) {
+        const int ti2 = i / p.nsteps, k = i - ti2 * p.nsteps;
+        const TbTap& tp = p.taps[t.tap_off + ti2];
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < TAP_C; ++q) {
+          const int rl = tp.rloc[q];
+          if (rl >= 0) acc = inj_acc(acc, tp.w[q], s_res[rl * p.tmax + k]);
+        }
+        x.s_tap[k * p.ntap_max + ti2] = acc;
+      }
+    }
+    x.mask = s_mask[x.tid];
+    x.base = s_base[x.tid];
+    x.srcsel = 0;
+    if (MODE != MODE_ADJ) {
+#pragma unroll
+      for (int j = 0; j < SRC_MAX; ++j) {
+        const int pos = s_srcpos[j];
+        if (pos >= 0 && (pos >> 8) == x.tid) x.srcsel |= 1u << j;
+      }
+    }
+    // run_item publishes the exchange rows and synchronises before the first step
+
+    if (t.flags) {
+      run_item<KY, MODE, true>(p, x);
+    } else {
+      run_item<KY, MODE, false>(p, x);
+    }
+
+    if (MODE == MODE_FWD) {
+      // receiver traces of the owned receivers, nsteps contiguous samples each
+      for (int i = x.tid; i < t.nrec * p.nsteps; i += nthr) {
+        const int j = i / p.nsteps, k = i - j * p.nsteps;
+        const TbRec& rc = p.recs[t.rec_off + j];
+        const float* v = x.s_tap + k * p.ntap_max;
+        const float smp = gather4(v[rc.slot[0]], v[rc.slot[1]], v[rc.slot[2]], v[rc.slot[3]],
+                                  rc.w[0], rc.w[1], rc.w[2], rc.w[3]);
+        p.traces[((long long)s * p.nrx + rc.rg) * p.nt + p.n0 + k] = smp;
+      }
+    }
+    if (MODE == MODE_ADJ) {
+      const float4* g4 = reinterpret_cast<const float4*>(x.s_g) + (x.w * KY) * 32 + x.lane;
+#pragma unroll
+      for (int r = 0; r < KY; ++r) {
+        if ((x.own_rows >> r) & 1u) {
+          const float4 gv = g4[r * 32];
+          double* gd = p.grad + (long long)(x.y0 + r) * p.pitch + x.xb;
+          if (x.own_cols & 1u) atomicAdd(gd + 0, (double)gv.x * p.scale);
+          if (x.own_cols & 2u) atomicAdd(gd + 1, (double)gv.y * p.scale);
+          if (x.own_cols & 4u) atomicAdd(gd + 2, (double)gv.z * p.scale);
+          if (x.own_cols & 8u) atomicAdd(gd + 3, (double)gv.w * p.scale);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int KY, int MODE>
+cudaError_t launch_one(const TbParams& p, int grid, size_t smem, cudaStream_t st) {
+  static bool configured = false;
+  static size_t configured_smem = 0;
+  if (!configured || smem > configured_smem) {
+    cudaError_t e = cudaFuncSetAttribute(tb_kernel<KY, MODE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+    configured_smem = smem;
+  }
+  tb_kernel<KY, MODE><<<grid, p.nwarps * 32, smem, st>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st) {
+  if (ky == 8) {
+    if (mode == MODE_FWD) return launch_one<8, MODE_FWD>(p, grid, smem, st);
+    if (mode == MODE_REC) return launch_one<8, MODE_REC>(p, grid, smem, st);
+    return launch_one<8, MODE_ADJ>(p, grid, smem, st);
+  }
+  if (mode == MODE_FWD) return launch_one<4, MODE_FWD>(p, grid, smem, st);
+  if (mode == MODE_REC) return launch_one<4, MODE_REC>(p, grid, smem, st);
+  return launch_one<4, MODE_ADJ>(p, grid, smem, st);
+}
+
+}  // namespace fdtd

@@ -1,0 +1,205 @@
+"""Device medium and fused-engine plans on top of the C ABI.
+
+``DeviceMedium`` holds one grid's float32 update coefficients and Mur
+coefficients in the padded device layout the kernels use. ``FusedPlan`` binds
+one execution plan of the temporally blocked engine (fixed grid, receivers,
+per-shot sources and step count) to a workspace owned by the PyTorch caching
+allocator, and runs the batched forward and the checkpointed adjoint.
+
+Layout: every field is float32 ``(shots, ny, pitch)`` with ``pitch`` the grid
+width rounded up to a multiple of 4; the padding columns hold zeros.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def padded_width(nx: int) -> int:
+    return (int(nx) + 3) // 4 * 4
+
+
+def require_cuda(device) -> torch.device:
+    device = torch.device(device)
+    if device.type != "cuda":
+        raise ValueError("The GB300 engine runs on CUDA devices only; got device "
+                         f"{device!s}. There is no CPU fallback.")
+    if not torch.cuda.is_available():
+        raise RuntimeError("CUDA is not available; the GB300 engine needs a GPU.")
+    return device
+
+
+def stream_handle(device=None) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def ptr(t) -> int:
+    return 0 if t is None else t.data_ptr()
+
+
+class DeviceMedium:
+    """Float32 coefficients (c dt)^2 and Mur edge coefficients of one grid."""
+
+    def __init__(self, c, dx, dy, dt, device):
+        self.device = require_cuda(device)
+        c64 = torch.as_tensor(c, dtype=torch.float64).to(self.device).contiguous()
+        if c64.ndim != 2:
+            raise ValueError("Sound speed c must be a 2D array (ny, nx).")
+        self.ny, self.nx = (int(s) for s in c64.shape)
+        self.pitch = padded_width(self.nx)
+        self.dx, self.dy, self.dt = float(dx), float(dy), float(dt)
+        self.c64 = c64
+        self.coef = torch.zeros((self.ny, self.pitch), dtype=torch.float32, device=self.device)
+        self.mur = torch.zeros(2 * self.ny + 2 * self.nx + 8, dtype=torch.float32, device=self.device)
+        self.prepare()
+
+    def set_c(self, c):
+        c64 = torch.as_tensor(c, dtype=torch.float64).to(self.device)
+        if tuple(c64.shape) != (self.ny, self.nx):
+            raise ValueError(f"Sound speed shape {tuple(c64.shape)} does not match {(self.ny, self.nx)}.")
+        self.c64.copy_(c64)
+        self.prepare()
+
+    def set_dt(self, dt):
+        self.dt = float(dt)
+        self.prepare()
+
+    def prepare(self):
+        lib = _lib.load()
+        _lib.check(lib.fdtd_prepare_medium(ptr(self.c64), self.ny, self.nx, self.pitch, self.dt,
+                                           self.dx, self.dy, ptr(self.coef), ptr(self.mur),
+                                           stream_handle(self.device)), "prepare_medium")
+
+    def grid(self) -> _lib.Grid:
+        return _lib.Grid(self.ny, self.nx, self.pitch, self.dx, self.dy, self.dt,
+                         ptr(self.coef), ptr(self.mur))
+
+    def new_field(self, n_shots=None):
+        shape = (self.ny, self.pitch) if n_shots is None else (int(n_shots), self.ny, self.pitch)
+        return torch.zeros(shape, dtype=torch.float32, device=self.device)
+
+
+class FusedPlan:
+    """One bound plan of the temporally blocked engine.
+
+    receivers: (row0, col0, weights (R, 4)); sources: rows, cols, weights and
+    waveform indices, each (S, K); waveforms: device float32 (n_waves, len).
+    """
+
+    def __init__(self, medium: DeviceMedium, receivers, sources, waveforms: torch.Tensor,
+                 n_steps: int, tuning: dict | None = None, for_gradient: bool = False):
+        self.medium = medium
+        self.lib = _lib.load()
+        row0, col0, w = receivers
+        self._rx_row0 = np.ascontiguousarray(row0, dtype=np.int32)
+        self._rx_col0 = np.ascontiguousarray(col0, dtype=np.int32)
+        self._rx_w = np.ascontiguousarray(w, dtype=np.float32).reshape(-1, 4)
+        rows, cols, sw, wave = (np.ascontiguousarray(a) for a in sources)
+        self._s_row = rows.astype(np.int32).reshape(rows.shape[0], -1)
+        self._s_col = cols.astype(np.int32).reshape(self._s_row.shape)
+        self._s_w = sw.astype(np.float32).reshape(self._s_row.shape)
+        self._s_wave = wave.astype(np.int32).reshape(self._s_row.shape)
+        if waveforms.dtype != torch.float32 or waveforms.device != medium.device or waveforms.ndim != 2:
+            raise ValueError("waveforms must be a float32 (n_waves, length) tensor on the engine device")
+        self.waveforms = waveforms.contiguous()
+        self.n_shots = int(self._s_row.shape[0])
+        self.n_rx = int(self._rx_row0.shape[0])
+        self.n_steps = int(n_steps)
+        self.for_gradient = bool(for_gradient)
+        self.problem = self._problem()
+        t = _lib.Tuning(**{k: int(v) for k, v in (tuning or {}).items()})
+        handle = ctypes.c_void_p()
+        _lib.check(self.lib.fdtd_plan_create(ctypes.byref(self.problem), ctypes.byref(t),
+                                             int(self.for_gradient), ctypes.byref(handle)), "plan")
+        self._plan = handle
+        nbytes = ctypes.c_size_t()
+        _lib.check(self.lib.fdtd_plan_workspace_bytes(self._plan, ctypes.byref(nbytes)))
+        self.workspace_bytes = int(nbytes.value)
+        self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=medium.device)
+        _lib.check(self.lib.fdtd_plan_bind(self._plan, ptr(self.workspace), self.workspace_bytes,
+                                           stream_handle(medium.device)), "bind")
+        resolved = _lib.Tuning()
+        _lib.check(self.lib.fdtd_plan_tuning(self._plan, ctypes.byref(resolved)))
+        self.tuning = resolved.as_dict()
+
+    def _problem(self) -> _lib.Problem:
+        m = self.medium
+        rx = _lib.Receivers(self.n_rx, self._rx_row0.ctypes.data, self._rx_col0.ctypes.data,
+                            self._rx_w.ctypes.data)
+        src = _lib.Sources(int(self._s_row.shape[1]), self._s_row.ctypes.data, self._s_col.ctypes.data,
+                           self._s_w.ctypes.data, self._s_wave.ctypes.data, ptr(self.waveforms),
+                           int(self.waveforms.shape[0]), int(self.waveforms.shape[1]))
+        return _lib.Problem(m.grid(), self.n_shots, self.n_steps, rx, src)
+
+    def set_waveforms(self, waveforms: torch.Tensor):
+        if tuple(waveforms.shape) != tuple(self.waveforms.shape):
+            raise ValueError("waveform shape changed; build a new plan")
+        self.waveforms.copy_(waveforms)
+
+    def refresh_medium(self):
+        """Re-point the plan at the medium's buffers (after DeviceMedium.prepare)."""
+        _lib.check(self.lib.fdtd_plan_set_medium(self._plan, ptr(self.medium.coef),
+                                                 ptr(self.medium.mur), ptr(self.waveforms)))
+
+    def forward(self, traces=None, u_prev_out=None, u_out=None, save_checkpoints=False):
+        """Run all shots for n_steps; returns traces (S, R, nt) float32."""
+        if traces is None:
+            traces = torch.empty((self.n_shots, self.n_rx, self.n_steps), dtype=torch.float32,
+                                 device=self.medium.device)
+        self.refresh_medium()
+        _lib.check(self.lib.fdtd_forward(self._plan, ptr(traces), ptr(u_prev_out), ptr(u_out),
+                                         int(bool(save_checkpoints)),
+                                         stream_handle(self.medium.device)), "forward")
+        return traces
+
+    def adjoint(self, residual: torch.Tensor, grad_c2: torch.Tensor):
+        """Add dt^2 sum_n adj^n lap(u^{n-1}) into grad_c2 (float64 (ny, pitch))."""
+        if residual.dtype != torch.float32 or not residual.is_contiguous():
+            raise ValueError("residual must be contiguous float32 (S, R, nt)")
+        if grad_c2.dtype != torch.float64 or tuple(grad_c2.shape) != (self.medium.ny, self.medium.pitch):
+            raise ValueError("grad_c2 must be float64 (ny, pitch)")
+        _lib.check(self.lib.fdtd_adjoint(self._plan, ptr(residual), ptr(grad_c2),
+                                         stream_handle(self.medium.device)), "adjoint")
+
+    def close(self):
+        if getattr(self, "_plan", None):
+            self.lib.fdtd_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def residual_misfit(traces, observed, mute, residual=None, misfit=None):
+    """residual = traces - observed (muted channel per shot) and 0.5 * sum(residual^2) in float64."""
+    lib = _lib.load()
+    S, R, nt = (int(v) for v in traces.shape)
+    if observed.shape[1:] != traces.shape[1:] or observed.stride(2) != 1 or observed.stride(1) != nt:
+        raise ValueError("observed must be (shots, receivers, steps) with contiguous rows")
+    if residual is None:
+        residual = torch.empty_like(traces)
+    if misfit is None:
+        misfit = torch.zeros(1, dtype=torch.float64, device=traces.device)
+    mute_t = None if mute is None else torch.as_tensor(mute, dtype=torch.int32, device=traces.device)
+    _lib.check(lib.fdtd_residual_misfit(S, R, nt, ptr(traces), ptr(observed), observed.stride(0),
+                                        ptr(mute_t), ptr(residual), ptr(misfit),
+                                        stream_handle(traces.device)), "residual")
+    return residual, misfit
+
+
+def chain_rule(grad_c2, m, mask=None):
+    """g_m = -g_{c^2} / m^2 on the mask (float64 device tensors of one shape)."""
+    lib = _lib.load()
+    out = torch.empty_like(m)
+    mk = None if mask is None else mask.to(torch.uint8).contiguous()
+    _lib.check(lib.fdtd_chain_rule(m.numel(), ptr(grad_c2.contiguous()), ptr(m.contiguous()), ptr(mk),
+                                   ptr(out), stream_handle(m.device)), "chain_rule")
+    return out

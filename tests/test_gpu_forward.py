@@ -1,0 +1,204 @@
+"""GPU parity of the forward path: one-step kernels and the fused engine.
+
+The oracle (float64 NumPy restatement of the reference, pinned to the
+reference's own outputs in test_oracle_golden.py) is the checker. Tolerances:
+traces rel-L2 <= 1e-5 against float64 (the spec trace budget), one-step
+kernels <= 1e-6; the fused engine and the one-step kernels run the same
+float32 arithmetic and must agree bit for bit.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import fdtd_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+TRACE_TOL = 1e-5
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+@pytest.fixture(scope="module")
+def tb():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from soundwavesimulation_gb300 import torch_backend
+    return torch_backend
+
+
+def geo_of(d):
+    g = {k: d[k] for k in ("row0", "col0", "w00", "w10", "w01", "w11")}
+    g["row1"] = g["row0"] + 1
+    g["col1"] = g["col0"] + 1
+    return g
+
+
+def ring41_objects(tb, golden, tuning=None):
+    from soundwavesimulation_gb300 import RingArray, axis_centers
+    d = golden("ring41")
+    x = axis_centers(41, float(d["dx"]))
+    model = tb.TorchScalarWave2D(d["c_true"], float(d["dx"]), device="cuda")
+    solver = tb.TorchFDTD2D(model, float(d["dt"]))
+    array = RingArray(6, 0.030, x, x)
+    sampler = tb.TorchRingSampler(array, device="cuda")
+    return d, solver, array, sampler
+
+
+def test_one_step_kernels_nonsquare(tb, golden):
+    """fdtd_step (forward and adjoint), gather, scatter and image vs the reference's single steps."""
+    from soundwavesimulation_gb300 import RingArray, axis_centers
+    d = golden("steps_nonsquare")
+    ny, nx = d["c"].shape
+    dx, dy, dt = float(d["dx"]), float(d["dy"]), float(d["dt"])
+    model = tb.TorchScalarWave2D(d["c"], dx, dy, device="cuda")
+    solver = tb.TorchFDTD2D(model, dt)
+    ring = RingArray(5, 0.0085, axis_centers(nx, dx), axis_centers(ny, dy))
+    sampler = tb.TorchRingSampler(ring, device="cuda")
+    batched = tb.TorchFDTD2DBatch(solver, 2)
+    batched.set_sources(d["src_rows"], d["src_cols"])
+    batched.u_old.copy_(torch.as_tensor(d["u_old0"]))
+    batched.u.copy_(torch.as_tensor(d["u0"]))
+    u, samples = batched.step_record(torch.tensor(float(d["src_value"]), device="cuda"), sampler)
+    assert rel(u.cpu(), d["fwd_u"]) < 1e-6
+    assert rel(samples.cpu(), d["fwd_samples"]) < 1e-6
+    batched.u_old.copy_(torch.as_tensor(d["u_old0"]))
+    batched.u.copy_(torch.as_tensor(d["u0"]))
+    g = batched.adjoint_step_image(torch.as_tensor(d["resid"], device="cuda"), sampler,
+                                   torch.as_tensor(d["fwd_field"], device="cuda"),
+                                   torch.as_tensor(d["g_in"], device="cuda"), float(d["image_scale"]))
+    assert rel(batched.u.cpu(), d["adj_u"]) < 1e-6
+    assert rel(g.cpu(), d["g_out"]) < 1e-6
+    solver.reset()
+    solver._rot.view(solver._rot.io).copy_(torch.as_tensor(d["u_old0"][0]))
+    solver._rot.view(solver._rot.ic).copy_(torch.as_tensor(d["u0"][0]))
+    single = solver.inject_field_and_step(torch.as_tensor(d["fwd_field"][0]), adjoint=True)
+    assert rel(single.cpu(), d["single_adj"]) < 1e-6
+
+
+def test_fused_ring41_matches_reference(tb, golden):
+    d, solver, array, sampler = ring41_objects(tb, golden)
+    nt = int(d["n_steps"])
+    traces, u = tb.simulate_shots_batch(solver, sampler, torch.as_tensor(d["pulse"]), array.rows,
+                                        array.cols, nt)
+    assert traces.shape == (6, 6, nt)
+    assert rel(traces.cpu(), d["observed"]) < TRACE_TOL
+    assert rel(u.cpu(), d["batched_u"]) < TRACE_TOL
+
+
+def test_single_shot_matches_reference(tb, golden):
+    d, solver, array, sampler = ring41_objects(tb, golden)
+    nt = int(d["n_steps"])
+    pulse = torch.as_tensor(d["pulse"], device="cuda")
+    fused, _ = tb.simulate_shot(solver, sampler, pulse, *array.inject_rows_cols(2), nt)
+    stepped, snaps = tb.simulate_shot(solver, sampler, pulse, *array.inject_rows_cols(2), nt,
+                                      snapshot_stride=50)
+    assert len(snaps) == (nt + 49) // 50
+    assert rel(fused.cpu(), d["observed"][2]) < TRACE_TOL
+    assert torch.equal(fused, stepped)  # fused engine == one-step kernels, bit for bit
+
+
+def test_fused_equals_per_step_bitwise(tb, golden):
+    d, solver, array, sampler = ring41_objects(tb, golden)
+    nt = int(d["n_steps"])
+    pulse = torch.as_tensor(d["pulse"], device="cuda", dtype=torch.float32)
+    traces, u = tb.simulate_shots_batch(solver, sampler, pulse, array.rows, array.cols, nt)
+    u = u.clone()
+    batched = tb.TorchFDTD2DBatch(solver, 6)
+    batched.set_sources(array.rows, array.cols)
+    batched.reset()
+    steps = []
+    zero = torch.zeros((), device="cuda")
+    for n in range(nt):
+        _, s = batched.step_record(pulse[n] if n < pulse.numel() else zero, sampler)
+        steps.append(s)
+    stepped = torch.stack(steps, dim=2)
+    assert torch.equal(traces, stepped)
+    assert torch.equal(u, batched.u)
+
+
+def test_ellipse_traces_against_float64(tb, golden):
+    from soundwavesimulation_gb300 import RingArray, axis_centers
+    d = golden("ellipses64")
+    n = d["c"].shape[0]
+    dx = float(d["dx"])
+    x = axis_centers(n, dx)
+    model = tb.TorchScalarWave2D(d["c"], dx, device="cuda")
+    solver = tb.TorchFDTD2D(model, float(d["dt"]))
+    ring = RingArray(16, 0.45 * n * dx, x, x)
+    sampler = tb.TorchRingSampler(ring, device="cuda")
+    tx = d["tx"]
+    wav = torch.as_tensor(d["wavelet"], dtype=torch.float32)
+    traces, _ = tb.simulate_shots_batch(solver, sampler, wav, ring.rows[tx], ring.cols[tx],
+                                        int(d["n_steps"]), source_values=wav)
+    assert rel(traces.cpu(), d["traces_f64"]) < TRACE_TOL
+
+
+def _random_problem(ny, nx, n_shots, n_rx, nt, seed, per_shot=1):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(1400.0, 1700.0, size=(ny, nx))
+    c[ny // 3: ny // 2, nx // 4: nx // 2] = 1900.0
+    dx, dy = 1.0e-3, 1.3e-3
+    dt = orc.stable_dt(2000.0, dx, dy, cfl=0.4)
+    row0 = rng.integers(0, ny - 1, size=n_rx)
+    col0 = rng.integers(0, nx - 1, size=n_rx)
+    wx = rng.uniform(0, 1, n_rx)
+    wy = rng.uniform(0, 1, n_rx)
+    w = np.stack([(1 - wx) * (1 - wy), wx * (1 - wy), (1 - wx) * wy, wx * wy], 1)
+    srow = rng.integers(1, ny - 1, size=(n_shots, per_shot))
+    scol = rng.integers(1, nx - 1, size=(n_shots, per_shot))
+    sw = rng.uniform(0.5, 1.5, size=(n_shots, per_shot))
+    wave = np.ones((n_shots, per_shot), dtype=np.int64)
+    t = np.arange(nt) * dt
+    waves = np.stack([np.sin(2e5 * t) * np.exp(-((t - 3e-5) / 1e-5) ** 2),
+                      np.cos(3e5 * t) * np.exp(-((t - 2e-5) / 8e-6) ** 2)])
+    return dict(c=c, dx=dx, dy=dy, dt=dt, row0=row0, col0=col0, w=w, srow=srow, scol=scol, sw=sw,
+                wave=wave, waves=waves)
+
+
+def _oracle_forward(p, nt):
+    ny, nx = p["c"].shape
+    geo = {"row0": p["row0"], "col0": p["col0"], "row1": p["row0"] + 1, "col1": p["col0"] + 1,
+           "w00": p["w"][:, 0], "w10": p["w"][:, 1], "w01": p["w"][:, 2], "w11": p["w"][:, 3]}
+    fields = orc.point_sources((ny, nx), p["srow"], p["scol"], p["sw"])
+    values = p["waves"][p["wave"][:, 0]]
+    traces, _, _, _ = orc.simulate_shots_batch(p["c"], p["dx"], p["dy"], p["dt"], geo, fields, values, nt)
+    return traces
+
+
+@pytest.mark.parametrize("ny,nx,shots,nt,tuning", [
+    (41, 37, 3, 90, {"steps_per_launch": 5}),
+    (67, 130, 2, 61, {"steps_per_launch": 7, "rows_per_lane": 4, "warps": 16}),
+    (150, 133, 2, 40, {"steps_per_launch": 12}),
+    (257, 261, 1, 33, {"steps_per_launch": 16, "warps": 12}),
+    (129, 128, 2, 25, {"steps_per_launch": 1}),
+    (200, 140, 2, 37, {"steps_per_launch": 3, "rows_per_lane": 4, "warps": 32}),
+])
+def test_fused_engine_shapes_and_tunings(tb, ny, nx, shots, nt, tuning):
+    """Odd sizes, several tiles, edge-straddling receivers, multi-node sources, every tuning family."""
+    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan
+    p = _random_problem(ny, nx, shots, 24, nt, seed=ny * 7 + nx, per_shot=2)
+    medium = DeviceMedium(p["c"], p["dx"], p["dy"], p["dt"], "cuda")
+    waves = torch.as_tensor(p["waves"], dtype=torch.float32, device="cuda")
+    wave_idx = np.stack([p["wave"][:, 0], 1 - p["wave"][:, 0]], 1)
+    plan = FusedPlan(medium, (p["row0"], p["col0"], p["w"]), (p["srow"], p["scol"], p["sw"], wave_idx),
+                     waves, nt, tuning=tuning)
+    traces = plan.forward().cpu().numpy()
+    q = dict(p)
+    geo = {"row0": p["row0"], "col0": p["col0"], "row1": p["row0"] + 1, "col1": p["col0"] + 1,
+           "w00": p["w"][:, 0], "w10": p["w"][:, 1], "w01": p["w"][:, 2], "w11": p["w"][:, 3]}
+    fields = np.zeros((shots, ny, nx))
+    ref = np.zeros_like(traces, dtype=np.float64)
+    # two waveforms per shot: superpose two oracle runs (the engine is linear in the sources)
+    for k in range(2):
+        fields = orc.point_sources((ny, nx), p["srow"][:, k:k + 1], p["scol"][:, k:k + 1], p["sw"][:, k:k + 1])
+        values = p["waves"][wave_idx[:, k]]
+        tr, _, _, _ = orc.simulate_shots_batch(p["c"], p["dx"], p["dy"], p["dt"], geo, fields, values, nt)
+        ref += tr
+    del q
+    assert rel(traces, ref) < TRACE_TOL
