@@ -31,6 +31,8 @@ def require_cuda(device) -> torch.device:
                          f"{device!s}. There is no CPU fallback.")
     if not torch.cuda.is_available():
         raise RuntimeError("CUDA is not available; the GB300 engine needs a GPU.")
+    if device.index is None:
+        device = torch.device("cuda", torch.cuda.current_device())
     return device
 
 
