@@ -160,9 +160,8 @@ def run_ours(args):
     torch.cuda.set_device(device)
     sys.path.insert(0, str(ROOT))
     from soundwavesimulation_gb300 import torch_backend as tb
-    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan
+    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan, ProblemTables, forward_plain
     from soundwavesimulation_gb300.phantoms import config
-    from soundwavesimulation_gb300 import _lib
 
     acq = config(2)[0]
     S, n, nt = acq.n_shots, acq.n, acq.n_steps
@@ -206,28 +205,12 @@ def run_ours(args):
     # plain per-shot form on a shot subset, scaled to the workload
     plain_shots = 2
     sub = acq.subset(n_shots=plain_shots)
-    prob = FusedPlan.__new__(FusedPlan)  # reuse the problem builder without a plan
-    prob.medium = medium
-    prob._rx_row0 = np.ascontiguousarray(rx[0], np.int32)
-    prob._rx_col0 = np.ascontiguousarray(rx[1], np.int32)
-    prob._rx_w = np.ascontiguousarray(rx[2], np.float32)
-    r_, c_, w_, wv_ = sub.source_tables()
-    prob._s_row, prob._s_col = r_.astype(np.int32), c_.astype(np.int32)
-    prob._s_w, prob._s_wave = w_.astype(np.float32), wv_.astype(np.int32)
-    prob.waveforms = waves
-    prob.n_shots, prob.n_rx, prob.n_steps = plain_shots, acq.n_elements, nt
-    problem = FusedPlan._problem(prob)
-    lib = _lib.load()
-    import ctypes
-    ws_bytes = lib.fdtd_forward_plain_workspace(ctypes.byref(problem))
-    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
-    ptraces = torch.empty((plain_shots, acq.n_elements, nt), dtype=torch.float32, device=device)
-    h = stream.cuda_stream
-    _lib.check(lib.fdtd_forward_plain(ctypes.byref(problem), ptraces.data_ptr(), ws.data_ptr(), ws_bytes, h))
+    tables = ProblemTables(medium, rx, sub.source_tables(), waves, nt)
+    ptraces = forward_plain(tables)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    _lib.check(lib.fdtd_forward_plain(ctypes.byref(problem), ptraces.data_ptr(), ws.data_ptr(), ws_bytes, h))
+    forward_plain(tables, ptraces)
     e1.record(stream)
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
@@ -289,13 +272,47 @@ def run_ours(args):
     return 0
 
 
+def run_profile(args):
+    """A small bounded run of one engine pass for profiler captures (no JSON line).
+
+    fwd: one batched forward; grad: forward with checkpoints + residual + adjoint
+    (recompute and adjoint kernels). Shots and steps are cut to --shots / --nt.
+    """
+    import torch
+    sys.path.insert(0, str(ROOT))
+    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan, residual_misfit
+    from soundwavesimulation_gb300.phantoms import config
+    device = torch.device("cuda", 0)
+    acq = config(2)[0].subset(n_shots=args.shots, n_steps=args.nt)
+    medium = DeviceMedium(acq.c, acq.dx, acq.dx, acq.dt, device)
+    waves = torch.as_tensor(acq.wavelet[None], dtype=torch.float32, device=device)
+    tuning = json.loads(args.tuning) if args.tuning else {}
+    plan = FusedPlan(medium, acq.ring.receiver_taps(), acq.source_tables(), waves, acq.n_steps,
+                     tuning=tuning, for_gradient=args.profile == "grad")
+    traces = plan.forward(save_checkpoints=args.profile == "grad")
+    if args.profile == "grad":
+        res, _ = residual_misfit(traces, torch.zeros_like(traces), None)
+        g = torch.zeros((medium.ny, medium.pitch), dtype=torch.float64, device=device)
+        plan.adjoint(res, g)
+    torch.cuda.synchronize()
+    print(f"profile {args.profile}: {acq.n_shots} shots, {acq.n_steps} steps, tuning {plan.tuning}")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--profile", choices=["fwd", "grad"], default=None,
+                    help="run one small engine pass for a profiler instead of the benchmark")
+    ap.add_argument("--shots", type=int, default=64)
+    ap.add_argument("--nt", type=int, default=36)
+    ap.add_argument("--tuning", default="", help="JSON engine tuning for --profile")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -45,11 +45,12 @@ enum {
 
 enum { FDTD_STORE_F32 = 0, FDTD_STORE_F16 = 1, FDTD_STORE_BF16 = 2 };
 
-/* Grid and medium. `coef` and `mur` come from fdtd_prepare_medium. */
+/* Grid and medium. `coef`, `diag` and `mur` come from fdtd_prepare_medium. */
 typedef struct fdtd_grid {
   int32_t ny, nx, pitch;
   double dx, dy, dt;
   const float* coef; /* device (ny, pitch): (c * dt)^2 */
+  const float* diag; /* device (ny, pitch): 2 - 2 (c * dt)^2 (1/dx^2 + 1/dy^2) */
   const float* mur;  /* device: k_left[ny], k_right[ny], k_bottom[nx], k_top[nx],
                         corner_kx[4], corner_ky[4] (corners in the order
                         (0,0), (0,nx-1), (ny-1,0), (ny-1,nx-1)) */
@@ -106,18 +107,19 @@ typedef struct fdtd_plan fdtd_plan; /* opaque host-side execution plan */
 int32_t fdtd_abi_version(void);
 const char* fdtd_last_error(void);
 
-/* Sound speed (device float64 (ny, nx), row stride nx) -> coef and Mur
+/* Sound speed (device float64 (ny, nx), row stride nx) -> coef, diag and Mur
    coefficients, computed in float64 and rounded to float32.
    Replaces TorchScalarWave2D.set_c (fdtd2d/torch_backend.py:158-168) and
    TorchFDTD2D._refresh_boundaries (fdtd2d/torch_backend.py:264-275). */
 int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pitch,
                             double dt, double dx, double dy,
-                            float* coef, float* mur, void* stream);
+                            float* coef, float* diag, float* mur, void* stream);
 
 /* ------------------------------------------------- one-step (plain) kernels */
 
 /* One leapfrog step for n_shots shots, Mur edges included:
      forward: u_next = 2u - u_old + coef * lap(u) + sources
+              (evaluated as diag * u - u_old + coef * (lap(u) - cdiag * u))
      adjoint: u_next = 2u - u_old + lap(coef * u) + sources
    Sources: `src_*` are device arrays of shape (n_shots, src_per_shot) (row, col,
    weight, waveform index) and inject w * waveforms[wave * waveform_len + step];
@@ -184,7 +186,7 @@ int32_t fdtd_plan_tuning(const fdtd_plan* plan, fdtd_tuning* tuning);
    tables into it; synchronises `stream` once. */
 int32_t fdtd_plan_bind(fdtd_plan* plan, void* workspace, size_t bytes, void* stream);
 /* Updates the medium and source waveform pointers of a bound plan (same shapes). */
-int32_t fdtd_plan_set_medium(fdtd_plan* plan, const float* coef, const float* mur,
+int32_t fdtd_plan_set_medium(fdtd_plan* plan, const float* coef, const float* diag, const float* mur,
                              const float* waveforms);
 
 /* Batched forward of every shot over n_steps with the fused temporally blocked
@@ -228,6 +230,18 @@ int32_t fdtd_chain_rule(int64_t n, const double* grad_c2, const double* m,
 int32_t fdtd_forward_plain(const fdtd_problem* problem, float* traces,
                            void* workspace, size_t bytes, void* stream);
 size_t fdtd_forward_plain_workspace(const fdtd_problem* problem);
+
+/* The plain per-shot gradient: for each shot a forward that keeps every field
+   (one step + one gather launch per step), the residual against `observed`
+   (device (n_shots, n_rx, n_steps)) with channel mute[s] zeroed, then one
+   scatter + adjoint step + imaging launch per step; adds the misfit into
+   misfit[0] and dt^2 sum adj^n lap(u^{n-1}) into grad_c2 (float64 (ny, pitch)).
+   The structure of TorchLeastSquaresFWI._adjoint_accumulate with full float32
+   history (invert_ring.py:668-681), on the one-step kernels. */
+int32_t fdtd_gradient_plain(const fdtd_problem* problem, const float* observed,
+                            const int32_t* mute, double* misfit, double* grad_c2,
+                            void* workspace, size_t bytes, void* stream);
+size_t fdtd_gradient_plain_workspace(const fdtd_problem* problem);
 
 /* ------------------------------------------------------- tiling (host) */
 

@@ -14,16 +14,23 @@ namespace fdtd {
 
 // ---------------------------------------------------------------- arithmetic
 
-// 5-point Laplacian (l + r) / dx^2 + (d + u) / dy^2 - 2 (1/dx^2 + 1/dy^2) c,
-// the conv2d kernel of fdtd2d/torch_backend.py:124-132.
-__device__ __forceinline__ float lap5(float c, float l, float r, float d, float u,
-                                      float idx2, float idy2, float cdiag) {
-  return __fmaf_rn(c, cdiag, __fmaf_rn(__fadd_rn(d, u), idy2, __fmul_rn(__fadd_rn(l, r), idx2)));
+// Off-centre part of the 5-point Laplacian, (l + r) / dx^2 + (d + u) / dy^2.
+__device__ __forceinline__ float nbr4(float l, float r, float d, float u, float idx2, float idy2) {
+  return __fmaf_rn(__fadd_rn(d, u), idy2, __fmul_rn(__fadd_rn(l, r), idx2));
 }
 
-// Forward leapfrog 2u - u_old + (c dt)^2 lap(u)  (fdtd2d/torch_backend.py:516).
-__device__ __forceinline__ float leap(float c, float p, float coef, float lap) {
-  return __fmaf_rn(coef, lap, __fsub_rn(__fadd_rn(c, c), p));
+// Full 5-point Laplacian nbr4 - 2 (1/dx^2 + 1/dy^2) c: the conv2d kernel of
+// fdtd2d/torch_backend.py:124-132 with zero padding.
+__device__ __forceinline__ float lap5(float c, float l, float r, float d, float u,
+                                      float idx2, float idy2, float cdiag) {
+  return __fmaf_rn(c, cdiag, nbr4(l, r, d, u, idx2, idy2));
+}
+
+// Forward leapfrog u+ = 2u - u_old + (c dt)^2 lap(u) (fdtd2d/torch_backend.py:516),
+// regrouped as a u - u_old + (c dt)^2 nbr4 with the per-cell a = 2 + (c dt)^2 cdiag
+// precomputed in float64: two fused multiply-adds after nbr4.
+__device__ __forceinline__ float leap(float c, float p, float a, float coef, float nb) {
+  return __fmaf_rn(coef, nb, __fmaf_rn(a, c, -p));
 }
 
 // Adjoint leapfrog 2l - l_old + lap((c dt)^2 l)  (fdtd2d/torch_backend.py:531-532);
@@ -100,7 +107,8 @@ struct TbParams {
   // grid
   int ny, nx, pitch;
   float idx2, idy2, cdiag;
-  const float* coef;
+  const float* coef;     // (c dt)^2
+  const float* diag;     // 2 + (c dt)^2 cdiag, forward update only
   const float* mur;
   // tiling
   const TbTile* tiles;
@@ -136,7 +144,7 @@ struct TbParams {
 // Dynamic shared-memory carve-up of the temporally blocked kernel; the host
 // sizes the launch with the same function.
 struct TbSmem {
-  size_t coef, g, xch, tap, res, src, mask, base, srcpos, total;
+  size_t coef, diag, g, xch, tap, res, src, mask, base, srcpos, total;
 };
 
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
@@ -147,6 +155,7 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
   const size_t region = size_t(nw) * ky * RX * sizeof(float);
   size_t off = 0;
   m.coef = off; off += region;
+  m.diag = off; if (mode != MODE_ADJ) off += region;
   m.g = off; if (mode == MODE_ADJ) off += region;
   m.xch = off; off += size_t(2) * nw * 2 * 32 * 16;
   m.tap = off; off += tb_align16(size_t(tmax) * (ntap_max > 0 ? ntap_max : 1) * sizeof(float));

@@ -129,7 +129,7 @@ int32_t validate_grid(const fdtd_grid& g) {
   if (g.ny < 8 || g.nx < 8) return fail(FDTD_ERR_INVALID, "grid must be at least 8 x 8");
   if (g.pitch < g.nx || g.pitch % 4 != 0) return fail(FDTD_ERR_INVALID, "pitch must be a multiple of 4 and >= nx");
   if (!(g.dx > 0) || !(g.dy > 0) || !(g.dt > 0)) return fail(FDTD_ERR_INVALID, "dx, dy and dt must be positive");
-  if (!g.coef || !g.mur) return fail(FDTD_ERR_INVALID, "coef and mur must be set");
+  if (!g.coef || !g.diag || !g.mur) return fail(FDTD_ERR_INVALID, "coef, diag and mur must be set");
   return FDTD_OK;
 }
 
@@ -144,6 +144,7 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.idy2 = (float)idy2;
   q.cdiag = (float)(-2.0 * (idx2 + idy2));
   q.coef = g.coef;
+  q.diag = g.diag;
   q.mur = g.mur;
   q.tiles = reinterpret_cast<const TbTile*>(p->ws + p->o_tiles);
   q.ntiles = (int)p->tiles.size();
@@ -402,10 +403,11 @@ int32_t fdtd_tap_table(int32_t ny, int32_t nx, const fdtd_receivers* rx, int32_t
 }
 
 int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pitch, double dt,
-                            double dx, double dy, float* coef, float* mur, void* stream) {
-  if (!c || !coef || !mur) return fail(FDTD_ERR_INVALID, "null pointer");
+                            double dx, double dy, float* coef, float* diag, float* mur, void* stream) {
+  if (!c || !coef || !diag || !mur) return fail(FDTD_ERR_INVALID, "null pointer");
   if (ny < 3 || nx < 3 || pitch < nx || pitch % 4) return fail(FDTD_ERR_INVALID, "bad grid shape");
-  cudaError_t e = prepare_medium_launch(c, ny, nx, pitch, dt, dx, dy, coef, mur, (cudaStream_t)stream);
+  if (!(dt > 0) || !(dx > 0) || !(dy > 0)) return fail(FDTD_ERR_INVALID, "dt, dx and dy must be positive");
+  cudaError_t e = prepare_medium_launch(c, ny, nx, pitch, dt, dx, dy, coef, diag, mur, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "prepare_medium");
   return FDTD_OK;
 }
@@ -423,6 +425,7 @@ int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, co
   if (n_shots < 1) return fail(FDTD_ERR_INVALID, "n_shots must be positive");
   if (src_per_shot > 0 && (!src_row || !src_col || !src_w || !src_wave || !waveforms))
     return fail(FDTD_ERR_INVALID, "source arrays missing");
+  if (!adjoint && !grid->diag) return fail(FDTD_ERR_INVALID, "diag must be set for the forward step");
   StepArgs a;
   a.ny = grid->ny;
   a.nx = grid->nx;
@@ -432,6 +435,7 @@ int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, co
   a.idy2 = (float)idy2;
   a.cdiag = (float)(-2.0 * (idx2 + idy2));
   a.coef = grid->coef;
+  a.diag = grid->diag;
   a.mur = grid->mur;
   a.n_shots = n_shots;
   a.u_old = u_old;
@@ -532,7 +536,23 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   const int max_warps = (t.rows_per_lane == 8) ? 16 : 32;
   if (t.warps == 0) t.warps = (t.rows_per_lane == 8) ? 16 : 32;
   if (t.warps < 2 || t.warps > max_warps) { delete p; return fail(FDTD_ERR_UNSUPPORTED, "warps out of range"); }
-  if (t.steps_per_launch == 0) t.steps_per_launch = 12;
+  if (t.steps_per_launch == 0) {
+    // Fewest computed cells per useful cell-update: tiles(T) * (T + 3) / T, where
+    // the 3 stands for the per-item load / setup / store cost in steps.
+    double best = 1e300;
+    int best_t = 8;
+    const int ry = t.rows_per_lane * t.warps;
+    for (int T = 4; T <= 32; ++T) {
+      std::vector<AxisTile> ax, ay;
+      if (!tile_axis(problem->grid.nx, RX, 4, T + 1, 0, ax).empty()) continue;
+      if (!tile_axis(problem->grid.ny, ry, 1, T + 1, t.rows_per_lane, ay).empty()) continue;
+      const int Teff = std::min(T, problem->n_steps);
+      const double cost = (double)ax.size() * ay.size() * (Teff + 3.0) / Teff;
+      if (cost <= best * (1.0 + 1e-9)) { best = cost; best_t = T; }
+      if (T >= problem->n_steps) break;
+    }
+    t.steps_per_launch = best_t;
+  }
   if (t.steps_per_launch < 1 || t.steps_per_launch > 48) { delete p; return fail(FDTD_ERR_UNSUPPORTED, "steps_per_launch must be in [1, 48]"); }
   if (t.ctas_per_sm == 0) t.ctas_per_sm = 1;
   if (t.ckpt_store < 0 || t.ckpt_store > 2) { delete p; return fail(FDTD_ERR_INVALID, "bad checkpoint storage type"); }
@@ -636,9 +656,11 @@ int32_t fdtd_plan_bind(fdtd_plan* p, void* workspace, size_t bytes, void* stream
   return FDTD_OK;
 }
 
-int32_t fdtd_plan_set_medium(fdtd_plan* p, const float* coef, const float* mur, const float* waveforms) {
+int32_t fdtd_plan_set_medium(fdtd_plan* p, const float* coef, const float* diag, const float* mur,
+                             const float* waveforms) {
   if (!p) return fail(FDTD_ERR_INVALID, "null plan");
   if (coef) p->prob.grid.coef = coef;
+  if (diag) p->prob.grid.diag = diag;
   if (mur) p->prob.grid.mur = mur;
   if (waveforms) p->prob.src.waveforms = waveforms;
   p->have_ckpt = false;
@@ -847,6 +869,106 @@ int32_t fdtd_forward_plain(const fdtd_problem* prob, float* traces, void* worksp
       if (rc) return rc;
       e = gather_launch(g.ny, g.pitch, 1, f[in], R, rx_rc, rx_w, traces + (size_t)s * R * nt + n, 0, nt, st);
       if (e != cudaSuccess) return cuda_fail(e, "plain gather");
+      const int t = io; io = ic; ic = in; in = t;
+    }
+  }
+  return FDTD_OK;
+}
+
+size_t fdtd_gradient_plain_workspace(const fdtd_problem* prob) {
+  if (!prob) return 0;
+  const size_t plane = (size_t)prob->grid.ny * prob->grid.pitch * sizeof(float);
+  const size_t R = prob->rx.n, nt = prob->n_steps;
+  return fdtd_forward_plain_workspace(prob) + align_up((nt + 2) * plane) + align_up(4 * plane) +
+         align_up(2 * R * nt * sizeof(float)) + align_up(4 * R * (10 + 8) * sizeof(int32_t));
+}
+
+int32_t fdtd_gradient_plain(const fdtd_problem* prob, const float* observed, const int32_t* mute,
+                            double* misfit, double* grad_c2, void* workspace, size_t bytes,
+                            void* stream) {
+  if (!prob || !observed || !misfit || !grad_c2) return fail(FDTD_ERR_INVALID, "null argument");
+  int32_t rc = validate_grid(prob->grid);
+  if (rc) return rc;
+  if (!workspace || bytes < fdtd_gradient_plain_workspace(prob)) return fail(FDTD_ERR_WORKSPACE, "workspace too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  const fdtd_grid& g = prob->grid;
+  const size_t plane = (size_t)g.ny * g.pitch;
+  const int R = prob->rx.n, S = prob->n_shots, nt = prob->n_steps;
+  const int K = prob->src.per_shot > 0 ? prob->src.per_shot : 0;
+  char* w = reinterpret_cast<char*>(workspace);
+  // shared pieces: receivers and sources (same layout as the plain forward)
+  size_t off = align_up(3 * plane * sizeof(float));
+  int32_t* rx_rc = reinterpret_cast<int32_t*>(w + off);
+  off += align_up((size_t)R * 2 * sizeof(int32_t));
+  float* rx_w = reinterpret_cast<float*>(w + off);
+  off += align_up((size_t)R * 4 * sizeof(float));
+  int32_t* s_row = reinterpret_cast<int32_t*>(w + off);
+  int32_t* s_col = s_row + (size_t)S * K;
+  int32_t* s_wave = s_col + (size_t)S * K;
+  float* s_w = reinterpret_cast<float*>(s_wave + (size_t)S * K);
+  off = fdtd_forward_plain_workspace(prob);
+  float* hist = reinterpret_cast<float*>(w + off);  // two zero planes, then u after every step
+  off += align_up((size_t)(nt + 2) * plane * sizeof(float));
+  float* lam = reinterpret_cast<float*>(w + off);   // three adjoint planes + the dense scatter plane
+  off += align_up(4 * plane * sizeof(float));
+  float* trace = reinterpret_cast<float*>(w + off);
+  float* resid = trace + (size_t)R * nt;
+  off += align_up(2 * (size_t)R * nt * sizeof(float));
+  int32_t* tap_nodes = reinterpret_cast<int32_t*>(w + off);
+  float* tap_w = reinterpret_cast<float*>(tap_nodes + (size_t)4 * R * 10);
+  std::vector<int32_t> nodes_h((size_t)4 * R * 10);
+  std::vector<float> tw_h((size_t)4 * R * 8);
+  int32_t n_nodes = 4 * R;
+  rc = fdtd_tap_table(g.ny, g.nx, &prob->rx, nodes_h.data(), tw_h.data(), &n_nodes);
+  if (rc) return rc;
+  std::vector<int32_t> rc_h(2 * (size_t)R);
+  for (int r = 0; r < R; ++r) { rc_h[2 * r] = prob->rx.row0[r]; rc_h[2 * r + 1] = prob->rx.col0[r]; }
+  cudaError_t e = cudaMemcpyAsync(rx_rc, rc_h.data(), rc_h.size() * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rx_w, prob->rx.w, (size_t)R * 16, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tap_nodes, nodes_h.data(), (size_t)n_nodes * 40, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tap_w, tw_h.data(), (size_t)n_nodes * 32, cudaMemcpyHostToDevice, st);
+  if (K > 0) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_row, prob->src.row, (size_t)S * K * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_col, prob->src.col, (size_t)S * K * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_wave, prob->src.wave, (size_t)S * K * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_w, prob->src.w, (size_t)S * K * 4, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "plain gradient upload");
+  const double idx2 = 1.0 / (g.dx * g.dx), idy2 = 1.0 / (g.dy * g.dy);
+  float* dense = lam + 3 * plane;
+  for (int s = 0; s < S; ++s) {
+    // forward with the whole history: hist[k + 2] holds u after step k
+    e = cudaMemsetAsync(hist, 0, 2 * plane * sizeof(float), st);
+    if (e != cudaSuccess) return cuda_fail(e, "plain gradient reset");
+    for (int n = 0; n < nt; ++n) {
+      float* un = hist + (size_t)(n + 2) * plane;
+      rc = fdtd_step(&g, 1, hist + (size_t)n * plane, hist + (size_t)(n + 1) * plane, un, K,
+                     s_row + (size_t)s * K, s_col + (size_t)s * K, s_w + (size_t)s * K,
+                     s_wave + (size_t)s * K, prob->src.waveforms, prob->src.waveform_len, n,
+                     nullptr, 0, stream);
+      if (rc) return rc;
+      e = gather_launch(g.ny, g.pitch, 1, un, R, rx_rc, rx_w, trace + n, 0, nt, st);
+      if (e != cudaSuccess) return cuda_fail(e, "plain gather");
+    }
+    e = residual_launch(1, R, nt, trace, observed + (size_t)s * R * nt, 0, mute ? mute + s : nullptr,
+                        resid, misfit, st);
+    if (e != cudaSuccess) return cuda_fail(e, "plain residual");
+    // reverse-time adjoint, one scatter + step + image launch per step
+    e = cudaMemsetAsync(lam, 0, 4 * plane * sizeof(float), st);
+    if (e != cudaSuccess) return cuda_fail(e, "plain adjoint reset");
+    int io = 0, ic = 1, in = 2;
+    for (int n = nt - 1; n >= 0; --n) {
+      e = scatter_launch(g.ny, g.pitch, 1, n_nodes, tap_nodes, tap_w, resid + n, 0, nt, dense, st);
+      if (e != cudaSuccess) return cuda_fail(e, "plain scatter");
+      rc = fdtd_step(&g, 1, lam + (size_t)io * plane, lam + (size_t)ic * plane, lam + (size_t)in * plane, 0,
+                     nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, dense, 1, stream);
+      if (rc) return rc;
+      if (n >= 1) {
+        e = image_launch(g.ny, g.nx, g.pitch, (float)idx2, (float)idy2, (float)(-2.0 * (idx2 + idy2)), 1,
+                         lam + (size_t)in * plane, hist + (size_t)(n + 1) * plane, g.dt * g.dt, grad_c2, st);
+        if (e != cudaSuccess) return cuda_fail(e, "plain image");
+      }
       const int t = io; io = ic; ic = in; in = t;
     }
   }

@@ -39,6 +39,7 @@ struct Ctx {
   unsigned mask, srcsel;
   int base;
   float* s_coef;
+  float* s_diag;
   float* s_g;
   float4* s_xch;
   float* s_tap;
@@ -59,6 +60,127 @@ __device__ __forceinline__ float4 ldg4(const float* p) {
   return __ldg(reinterpret_cast<const float4*>(p));
 }
 
+// Mur edges and corners, in registers (plus shuffles across one lane boundary).
+// The tiler places rows 0/1 and ny-2/ny-1 in one band and column 0 at lane 0, c = 0.
+// Cells outside the domain need no treatment: their coef and diag are zero, so
+// in the forward they stay exactly zero (u+ = 0 * u - u_old + 0 starting from
+// zero), and in the adjoint their operand coef * l is zero, so whatever they
+// hold never reaches a domain cell and they are never written back.
+template <int KY>
+__device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY][4],
+                                         const TbParams& p, const Ctx& x) {
+  const int nx = p.nx, ny = p.ny;
+  const float* kl = p.mur;
+  const float* kr = kl + ny;
+  const float* kb = kr + ny;
+  const float* kt = kb + nx;
+  const float* ckx = kt + nx;
+  const float* cky = ckx + 4;
+  const int rb = -x.y0;          // band row of global row 0
+  const int rt = ny - 1 - x.y0;  // band row of global row ny-1
+  const bool has_bot = (x.flags & TF_BOTTOM) && rb >= 0 && rb + 1 < KY;   // warp-uniform
+  const bool has_top = (x.flags & TF_TOP) && rt >= 1 && rt < KY;          // warp-uniform
+  if (has_bot) {
+#pragma unroll
+    for (int r = 0; r + 1 < KY; ++r) {
+      if (r == rb) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int xx = x.xb + c;
+          if (xx >= 1 && xx <= nx - 2) P[r][c] = mur(C[r + 1][c], __ldg(kb + xx), P[r + 1][c], C[r][c]);
+        }
+      }
+    }
+  }
+  if (has_top) {
+#pragma unroll
+    for (int r = 1; r < KY; ++r) {
+      if (r == rt) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int xx = x.xb + c;
+          if (xx >= 1 && xx <= nx - 2) P[r][c] = mur(C[r - 1][c], __ldg(kt + xx), P[r - 1][c], C[r][c]);
+        }
+      }
+    }
+  }
+  if ((x.flags & TF_LEFT) && x.lane == 0) {
+#pragma unroll
+    for (int r = 0; r < KY; ++r) {
+      const int yy = x.y0 + r;
+      if (yy >= 1 && yy <= ny - 2) P[r][0] = mur(C[r][1], __ldg(kl + yy), P[r][1], C[r][0]);
+    }
+  }
+  if (x.flags & TF_RIGHT) {
+    const int lx1 = nx - 1 - x.rx0;
+    const int L1 = lx1 >> 2, c1 = lx1 & 3;
+    // Column nx-2 sits in the same lane (c1 >= 1) or in column 3 of the previous
+    // lane (c1 == 0, one shuffle pair per row, executed by the whole warp). The
+    // edge rows are updated first, so the corners below see updated values.
+#pragma unroll
+    for (int r = 0; r < KY; ++r) {
+      float su = 0.f, sn = 0.f;
+      if (c1 == 0) {
+        su = __shfl_up_sync(FULL, C[r][3], 1);
+        sn = __shfl_up_sync(FULL, P[r][3], 1);
+      }
+      const int yy = x.y0 + r;
+      if (x.lane == L1 && yy >= 1 && yy <= ny - 2) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (c == c1) {
+            const float uin = (c == 0) ? su : C[r][c > 0 ? c - 1 : 0];
+            const float nin = (c == 0) ? sn : P[r][c > 0 ? c - 1 : 0];
+            P[r][c] = mur(uin, __ldg(kr + yy), nin, C[r][c]);
+          }
+        }
+      }
+    }
+    if (has_bot || has_top) {  // corners (0, nx-1) and (ny-1, nx-1)
+#pragma unroll
+      for (int r = 0; r < KY; ++r) {
+        const bool bot = has_bot && r == rb;
+        const bool top = has_top && r == rt;
+        if (bot || top) {  // warp-uniform
+          float su = 0.f, sn = 0.f;
+          if (c1 == 0) {
+            su = __shfl_up_sync(FULL, C[r][3], 1);
+            sn = __shfl_up_sync(FULL, P[r][3], 1);
+          }
+          if (x.lane == L1) {
+            const int rn = bot ? (r + 1 < KY ? r + 1 : r) : (r >= 1 ? r - 1 : r);
+            const int ci = bot ? 1 : 3;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (c == c1) {
+                const float uin = (c == 0) ? su : C[r][c > 0 ? c - 1 : 0];
+                const float nin = (c == 0) ? sn : P[r][c > 0 ? c - 1 : 0];
+                const float fx = mur(uin, __ldg(ckx + ci), nin, C[r][c]);
+                const float fy = mur(C[rn][c], __ldg(cky + ci), P[rn][c], C[r][c]);
+                P[r][c] = corner_avg(fx, fy);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  if ((x.flags & TF_LEFT) && x.lane == 0 && (has_bot || has_top)) {  // corners (0, 0), (ny-1, 0)
+#pragma unroll
+    for (int r = 0; r < KY; ++r) {
+      const bool bot = has_bot && r == rb;
+      const bool top = has_top && r == rt;
+      if (bot || top) {
+        const int rn = bot ? (r + 1 < KY ? r + 1 : r) : (r >= 1 ? r - 1 : r);
+        const int ci = bot ? 0 : 2;
+        const float fx = mur(C[r][1], __ldg(ckx + ci), P[r][1], C[r][0]);
+        const float fy = mur(C[rn][0], __ldg(cky + ci), P[rn][0], C[r][0]);
+        P[r][0] = corner_avg(fx, fy);
+      }
+    }
+  }
+}
+
 template <int KY, int MODE, bool EDGE>
 __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
                                         const TbParams& p, const Ctx& x, int k) {
@@ -67,6 +189,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   const float4* xin = x.s_xch + (k & 1) * x.nw * 64;
   float4* xout = x.s_xch + ((k + 1) & 1) * x.nw * 64;
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
+  const float4* diag4 = reinterpret_cast<const float4*>(x.s_diag) + (x.w * KY) * 32 + x.lane;
   const float idx2 = p.idx2, idy2 = p.idy2, cdiag = p.cdiag;
 
   // ---- stencil over the band, rolling the row above / below
@@ -87,32 +210,35 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
     float rgt = __shfl_down_sync(FULL, cur.x, 1);
     if (lzero) lft = 0.f;
     if (rzero) rgt = 0.f;
-    const float l0 = lap5(cur.x, lft, cur.y, prv.x, nxt.x, idx2, idy2, cdiag);
-    const float l1 = lap5(cur.y, cur.x, cur.z, prv.y, nxt.y, idx2, idy2, cdiag);
-    const float l2 = lap5(cur.z, cur.y, cur.w, prv.z, nxt.z, idx2, idy2, cdiag);
-    const float l3 = lap5(cur.w, cur.z, rgt, prv.w, nxt.w, idx2, idy2, cdiag);
+    const float n0 = nbr4(lft, cur.y, prv.x, nxt.x, idx2, idy2);
+    const float n1 = nbr4(cur.x, cur.z, prv.y, nxt.y, idx2, idy2);
+    const float n2 = nbr4(cur.y, cur.w, prv.z, nxt.z, idx2, idy2);
+    const float n3 = nbr4(cur.z, rgt, prv.w, nxt.w, idx2, idy2);
     if (MODE == MODE_ADJ) {
-      P[r][0] = leap_adj(C[r][0], P[r][0], l0);
-      P[r][1] = leap_adj(C[r][1], P[r][1], l1);
-      P[r][2] = leap_adj(C[r][2], P[r][2], l2);
-      P[r][3] = leap_adj(C[r][3], P[r][3], l3);
+      P[r][0] = leap_adj(C[r][0], P[r][0], __fmaf_rn(cur.x, cdiag, n0));
+      P[r][1] = leap_adj(C[r][1], P[r][1], __fmaf_rn(cur.y, cdiag, n1));
+      P[r][2] = leap_adj(C[r][2], P[r][2], __fmaf_rn(cur.z, cdiag, n2));
+      P[r][3] = leap_adj(C[r][3], P[r][3], __fmaf_rn(cur.w, cdiag, n3));
     } else {
       const float4 co = coef4[r * 32];
-      P[r][0] = leap(C[r][0], P[r][0], co.x, l0);
-      P[r][1] = leap(C[r][1], P[r][1], co.y, l1);
-      P[r][2] = leap(C[r][2], P[r][2], co.z, l2);
-      P[r][3] = leap(C[r][3], P[r][3], co.w, l3);
-    }
-    if (MODE == MODE_REC && ((x.own_rows >> r) & 1u)) {
-      float* dst = segrow + (long long)r * p.pitch;
-      if (x.own_cols == 0xFu) {
-        *reinterpret_cast<float4*>(dst) = make_float4(l0, l1, l2, l3);
-      } else {
-        if (x.own_cols & 1u) dst[0] = l0;
-        if (x.own_cols & 2u) dst[1] = l1;
-        if (x.own_cols & 4u) dst[2] = l2;
-        if (x.own_cols & 8u) dst[3] = l3;
+      const float4 dg = diag4[r * 32];
+      if (MODE == MODE_REC && ((x.own_rows >> r) & 1u)) {
+        const float l0 = __fmaf_rn(cur.x, cdiag, n0), l1 = __fmaf_rn(cur.y, cdiag, n1);
+        const float l2 = __fmaf_rn(cur.z, cdiag, n2), l3 = __fmaf_rn(cur.w, cdiag, n3);
+        float* dst = segrow + (long long)r * p.pitch;
+        if (x.own_cols == 0xFu) {
+          *reinterpret_cast<float4*>(dst) = make_float4(l0, l1, l2, l3);
+        } else {
+          if (x.own_cols & 1u) dst[0] = l0;
+          if (x.own_cols & 2u) dst[1] = l1;
+          if (x.own_cols & 4u) dst[2] = l2;
+          if (x.own_cols & 8u) dst[3] = l3;
+        }
       }
+      P[r][0] = leap(C[r][0], P[r][0], dg.x, co.x, n0);
+      P[r][1] = leap(C[r][1], P[r][1], dg.y, co.y, n1);
+      P[r][2] = leap(C[r][2], P[r][2], dg.z, co.z, n2);
+      P[r][3] = leap(C[r][3], P[r][3], dg.w, co.w, n3);
     }
     prv = cur;
     cur = nxt;
@@ -144,121 +270,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
 
   // ---- Mur edges and corners, zero outside the domain
-  if (EDGE) {
-    const int nx = p.nx, ny = p.ny;
-    const float* kl = p.mur;
-    const float* kr = kl + ny;
-    const float* kb = kr + ny;
-    const float* kt = kb + nx;
-    const float* ckx = kt + nx;
-    const float* cky = ckx + 4;
-    const int rb = -x.y0;            // local row of global row 0
-    const int rt = ny - 1 - x.y0;    // local row of global row ny-1
-    if (x.flags & TF_BOTTOM) {
-#pragma unroll
-      for (int r = 0; r + 1 < KY; ++r) {
-        if (r == rb) {
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const int xx = x.xb + c;
-            if (xx >= 1 && xx <= nx - 2) P[r][c] = mur(C[r + 1][c], __ldg(kb + xx), P[r + 1][c], C[r][c]);
-          }
-        }
-      }
-    }
-    if (x.flags & TF_TOP) {
-#pragma unroll
-      for (int r = 1; r < KY; ++r) {
-        if (r == rt) {
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const int xx = x.xb + c;
-            if (xx >= 1 && xx <= nx - 2) P[r][c] = mur(C[r - 1][c], __ldg(kt + xx), P[r - 1][c], C[r][c]);
-          }
-        }
-      }
-    }
-    if ((x.flags & TF_LEFT) && x.lane == 0) {  // the tiler puts column 0 at lane 0, c = 0
-#pragma unroll
-      for (int r = 0; r < KY; ++r) {
-        const int yy = x.y0 + r;
-        if (yy >= 1 && yy <= ny - 2) P[r][0] = mur(C[r][1], __ldg(kl + yy), P[r][1], C[r][0]);
-      }
-    }
-    if (x.flags & TF_RIGHT) {
-      const int lx1 = nx - 1 - x.rx0;
-      const int L1 = lx1 >> 2, c1 = lx1 & 3;
-      // Values of column nx-2 at this lane's rows: same lane (c1 >= 1) or the
-      // previous lane's column 3 (c1 == 0). Taken after the row-0/ny-1 updates so
-      // the corners below see the updated edge values.
-      float su[KY], sn[KY];
-#pragma unroll
-      for (int r = 0; r < KY; ++r) {
-        su[r] = __shfl_up_sync(FULL, C[r][3], 1);
-        sn[r] = __shfl_up_sync(FULL, P[r][3], 1);
-      }
-      if (x.lane == L1) {
-#pragma unroll
-        for (int r = 0; r < KY; ++r) {
-          const int yy = x.y0 + r;
-          if (yy >= 1 && yy <= ny - 2) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              if (c == c1) {
-                const float uin = (c == 0) ? su[r] : C[r][c > 0 ? c - 1 : 0];
-                const float nin = (c == 0) ? sn[r] : P[r][c > 0 ? c - 1 : 0];
-                P[r][c] = mur(uin, __ldg(kr + yy), nin, C[r][c]);
-              }
-            }
-          }
-        }
-        // corners (0, nx-1) and (ny-1, nx-1)
-#pragma unroll
-        for (int r = 0; r < KY; ++r) {
-          const bool bot = (x.flags & TF_BOTTOM) && r == rb && r + 1 < KY;
-          const bool top = (x.flags & TF_TOP) && r == rt && r >= 1;
-          if (bot || top) {
-            const int rn = bot ? (r + 1 < KY ? r + 1 : r) : (r >= 1 ? r - 1 : r);
-            const int ci = bot ? 1 : 3;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              if (c == c1) {
-                const float uin = (c == 0) ? su[r] : C[r][c > 0 ? c - 1 : 0];
-                const float nin = (c == 0) ? sn[r] : P[r][c > 0 ? c - 1 : 0];
-                const float fx = mur(uin, __ldg(ckx + ci), nin, C[r][c]);
-                const float fy = mur(C[rn][c], __ldg(cky + ci), P[rn][c], C[r][c]);
-                P[r][c] = corner_avg(fx, fy);
-              }
-            }
-          }
-        }
-      }
-    }
-    if ((x.flags & TF_LEFT) && x.lane == 0) {  // corners (0, 0) and (ny-1, 0)
-#pragma unroll
-      for (int r = 0; r < KY; ++r) {
-        const bool bot = (x.flags & TF_BOTTOM) && r == rb && r + 1 < KY;
-        const bool top = (x.flags & TF_TOP) && r == rt && r >= 1;
-        if (bot || top) {
-          const int rn = bot ? (r + 1 < KY ? r + 1 : r) : (r >= 1 ? r - 1 : r);
-          const int ci = bot ? 0 : 2;
-          const float fx = mur(C[r][1], __ldg(ckx + ci), P[r][1], C[r][0]);
-          const float fy = mur(C[rn][0], __ldg(cky + ci), P[rn][0], C[r][0]);
-          P[r][0] = corner_avg(fx, fy);
-        }
-      }
-    }
-    if (x.flags & TF_OUTSIDE) {
-#pragma unroll
-      for (int r = 0; r < KY; ++r) {
-        const int yy = x.y0 + r;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          if (yy < 0 || yy >= ny || x.xb + c >= nx) P[r][c] = 0.f;
-        }
-      }
-    }
-  }
+  if (EDGE) boundary<KY>(P, C, p, x);
 
   // ---- receiver taps (forward) / imaging (adjoint)
   if (MODE == MODE_FWD && x.mask) {
@@ -272,7 +284,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
       }
     }
   }
-  if (MODE == MODE_ADJ && n >= 1) {
+  if (MODE == MODE_ADJ && n >= 1 && x.own_rows && x.own_cols) {
     const float* sl = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
                       ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
     float4* g4 = reinterpret_cast<float4*>(x.s_g) + (x.w * KY) * 32 + x.lane;
@@ -308,6 +320,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
 template <int KY>
 __device__ __forceinline__ void store_state(const TbParams& p, const Ctx& x,
                                             const float (&prev)[KY][4], const float (&cur)[KY][4]) {
+  if (!x.own_rows || !x.own_cols) return;
   const long long base = ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
 #pragma unroll
   for (int r = 0; r < KY; ++r) {
@@ -344,12 +357,6 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
     }
     P[r][0] = a.x; P[r][1] = a.y; P[r][2] = a.z; P[r][3] = a.w;
     C[r][0] = b.x; C[r][1] = b.y; C[r][2] = b.z; C[r][3] = b.w;
-    if (EDGE) {
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        if (x.xb + c >= p.nx) { P[r][c] = 0.f; C[r][c] = 0.f; }
-      }
-    }
   }
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
   x.s_xch[x.w * 64 + x.lane] = opval<MODE>(C[0], coef4[0]);
@@ -379,6 +386,7 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
   x.lane = x.tid & 31;
   x.nw = nw;
   x.s_coef = reinterpret_cast<float*>(smem + L.coef);
+  x.s_diag = reinterpret_cast<float*>(smem + L.diag);
   x.s_g = reinterpret_cast<float*>(smem + L.g);
   x.s_xch = reinterpret_cast<float4*>(smem + L.xch);
   x.s_tap = reinterpret_cast<float*>(smem + L.tap);
@@ -419,14 +427,19 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
       const int yy = x.y0 + r;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (yy >= 0 && yy < p.ny && x.xb < p.pitch) v = ldg4(p.coef + (long long)yy * p.pitch + x.xb);
-      if (x.xb + 0 >= p.nx) v.x = 0.f;
-      if (x.xb + 1 >= p.nx) v.y = 0.f;
-      if (x.xb + 2 >= p.nx) v.z = 0.f;
-      if (x.xb + 3 >= p.nx) v.w = 0.f;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f), d = v;
+      if (yy >= 0 && yy < p.ny && x.xb < p.pitch) {
+        v = ldg4(p.coef + (long long)yy * p.pitch + x.xb);
+        if (MODE != MODE_ADJ) d = ldg4(p.diag + (long long)yy * p.pitch + x.xb);
+      }
+      if (x.xb + 0 >= p.nx) { v.x = 0.f; d.x = 0.f; }
+      if (x.xb + 1 >= p.nx) { v.y = 0.f; d.y = 0.f; }
+      if (x.xb + 2 >= p.nx) { v.z = 0.f; d.z = 0.f; }
+      if (x.xb + 3 >= p.nx) { v.w = 0.f; d.w = 0.f; }
       reinterpret_cast<float4*>(x.s_coef)[(x.w * KY + r) * 32 + x.lane] = v;
-      if (MODE == MODE_ADJ) {
+      if (MODE != MODE_ADJ) {
+        reinterpret_cast<float4*>(x.s_diag)[(x.w * KY + r) * 32 + x.lane] = d;
+      } else {
         reinterpret_cast<float4*>(x.s_g)[(x.w * KY + r) * 32 + x.lane] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
@@ -516,7 +529,7 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
         p.traces[((long long)s * p.nrx + rc.rg) * p.nt + p.n0 + k] = smp;
       }
     }
-    if (MODE == MODE_ADJ) {
+    if (MODE == MODE_ADJ && x.own_rows && x.own_cols) {
       const float4* g4 = reinterpret_cast<const float4*>(x.s_g) + (x.w * KY) * 32 + x.lane;
 #pragma unroll
       for (int r = 0; r < KY; ++r) {
@@ -536,13 +549,11 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
 
 template <int KY, int MODE>
 cudaError_t launch_one(const TbParams& p, int grid, size_t smem, cudaStream_t st) {
-  static bool configured = false;
   static size_t configured_smem = 0;
-  if (!configured || smem > configured_smem) {
+  if (smem > configured_smem) {
     cudaError_t e = cudaFuncSetAttribute(tb_kernel<KY, MODE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    configured = true;
     configured_smem = smem;
   }
   tb_kernel<KY, MODE><<<grid, p.nwarps * 32, smem, st>>>(p);

@@ -57,6 +57,7 @@ class DeviceMedium:
         self.dx, self.dy, self.dt = float(dx), float(dy), float(dt)
         self.c64 = c64
         self.coef = torch.zeros((self.ny, self.pitch), dtype=torch.float32, device=self.device)
+        self.diag = torch.zeros((self.ny, self.pitch), dtype=torch.float32, device=self.device)
         self.mur = torch.zeros(2 * self.ny + 2 * self.nx + 8, dtype=torch.float32, device=self.device)
         self.prepare()
 
@@ -74,29 +75,27 @@ class DeviceMedium:
     def prepare(self):
         lib = _lib.load()
         _lib.check(lib.fdtd_prepare_medium(ptr(self.c64), self.ny, self.nx, self.pitch, self.dt,
-                                           self.dx, self.dy, ptr(self.coef), ptr(self.mur),
-                                           stream_handle(self.device)), "prepare_medium")
+                                           self.dx, self.dy, ptr(self.coef), ptr(self.diag),
+                                           ptr(self.mur), stream_handle(self.device)), "prepare_medium")
 
     def grid(self) -> _lib.Grid:
         return _lib.Grid(self.ny, self.nx, self.pitch, self.dx, self.dy, self.dt,
-                         ptr(self.coef), ptr(self.mur))
+                         ptr(self.coef), ptr(self.diag), ptr(self.mur))
 
     def new_field(self, n_shots=None):
         shape = (self.ny, self.pitch) if n_shots is None else (int(n_shots), self.ny, self.pitch)
         return torch.zeros(shape, dtype=torch.float32, device=self.device)
 
 
-class FusedPlan:
-    """One bound plan of the temporally blocked engine.
+class ProblemTables:
+    """Host description of one acquisition for the C ABI (keeps the host arrays alive).
 
     receivers: (row0, col0, weights (R, 4)); sources: rows, cols, weights and
     waveform indices, each (S, K); waveforms: device float32 (n_waves, len).
     """
 
-    def __init__(self, medium: DeviceMedium, receivers, sources, waveforms: torch.Tensor,
-                 n_steps: int, tuning: dict | None = None, for_gradient: bool = False):
+    def __init__(self, medium: DeviceMedium, receivers, sources, waveforms: torch.Tensor, n_steps: int):
         self.medium = medium
-        self.lib = _lib.load()
         row0, col0, w = receivers
         self._rx_row0 = np.ascontiguousarray(row0, dtype=np.int32)
         self._rx_col0 = np.ascontiguousarray(col0, dtype=np.int32)
@@ -112,11 +111,61 @@ class FusedPlan:
         self.n_shots = int(self._s_row.shape[0])
         self.n_rx = int(self._rx_row0.shape[0])
         self.n_steps = int(n_steps)
+
+    def problem(self) -> _lib.Problem:
+        m = self.medium
+        rx = _lib.Receivers(self.n_rx, self._rx_row0.ctypes.data, self._rx_col0.ctypes.data,
+                            self._rx_w.ctypes.data)
+        src = _lib.Sources(int(self._s_row.shape[1]), self._s_row.ctypes.data, self._s_col.ctypes.data,
+                           self._s_w.ctypes.data, self._s_wave.ctypes.data, ptr(self.waveforms),
+                           int(self.waveforms.shape[0]), int(self.waveforms.shape[1]))
+        return _lib.Problem(m.grid(), self.n_shots, self.n_steps, rx, src)
+
+
+def forward_plain(tables: ProblemTables, traces=None):
+    """The plain per-shot form: one step + one gather launch per step, shot after shot."""
+    lib = _lib.load()
+    prob = tables.problem()
+    nbytes = int(lib.fdtd_forward_plain_workspace(ctypes.byref(prob)))
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=tables.medium.device)
+    if traces is None:
+        traces = torch.empty((tables.n_shots, tables.n_rx, tables.n_steps), dtype=torch.float32,
+                             device=tables.medium.device)
+    _lib.check(lib.fdtd_forward_plain(ctypes.byref(prob), ptr(traces), ptr(ws), nbytes,
+                                      stream_handle(tables.medium.device)), "forward_plain")
+    return traces
+
+
+def gradient_plain(tables: ProblemTables, observed, mute, grad_c2=None, misfit=None):
+    """The plain per-shot gradient (full float32 history, one launch per kernel per step)."""
+    lib = _lib.load()
+    prob = tables.problem()
+    dev = tables.medium.device
+    nbytes = int(lib.fdtd_gradient_plain_workspace(ctypes.byref(prob)))
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    if grad_c2 is None:
+        grad_c2 = torch.zeros((tables.medium.ny, tables.medium.pitch), dtype=torch.float64, device=dev)
+    if misfit is None:
+        misfit = torch.zeros(1, dtype=torch.float64, device=dev)
+    mute_t = None if mute is None else torch.as_tensor(mute, dtype=torch.int32, device=dev)
+    observed = observed.to(device=dev, dtype=torch.float32).contiguous()
+    _lib.check(lib.fdtd_gradient_plain(ctypes.byref(prob), ptr(observed), ptr(mute_t), ptr(misfit),
+                                       ptr(grad_c2), ptr(ws), nbytes, stream_handle(dev)), "gradient_plain")
+    return misfit, grad_c2
+
+
+class FusedPlan(ProblemTables):
+    """One bound plan of the temporally blocked engine over a ProblemTables acquisition."""
+
+    def __init__(self, medium: DeviceMedium, receivers, sources, waveforms: torch.Tensor,
+                 n_steps: int, tuning: dict | None = None, for_gradient: bool = False):
+        super().__init__(medium, receivers, sources, waveforms, n_steps)
+        self.lib = _lib.load()
         self.for_gradient = bool(for_gradient)
-        self.problem = self._problem()
+        self._problem_struct = self.problem()
         t = _lib.Tuning(**{k: int(v) for k, v in (tuning or {}).items()})
         handle = ctypes.c_void_p()
-        _lib.check(self.lib.fdtd_plan_create(ctypes.byref(self.problem), ctypes.byref(t),
+        _lib.check(self.lib.fdtd_plan_create(ctypes.byref(self._problem_struct), ctypes.byref(t),
                                              int(self.for_gradient), ctypes.byref(handle)), "plan")
         self._plan = handle
         nbytes = ctypes.c_size_t()
@@ -129,15 +178,6 @@ class FusedPlan:
         _lib.check(self.lib.fdtd_plan_tuning(self._plan, ctypes.byref(resolved)))
         self.tuning = resolved.as_dict()
 
-    def _problem(self) -> _lib.Problem:
-        m = self.medium
-        rx = _lib.Receivers(self.n_rx, self._rx_row0.ctypes.data, self._rx_col0.ctypes.data,
-                            self._rx_w.ctypes.data)
-        src = _lib.Sources(int(self._s_row.shape[1]), self._s_row.ctypes.data, self._s_col.ctypes.data,
-                           self._s_w.ctypes.data, self._s_wave.ctypes.data, ptr(self.waveforms),
-                           int(self.waveforms.shape[0]), int(self.waveforms.shape[1]))
-        return _lib.Problem(m.grid(), self.n_shots, self.n_steps, rx, src)
-
     def set_waveforms(self, waveforms: torch.Tensor):
         if tuple(waveforms.shape) != tuple(self.waveforms.shape):
             raise ValueError("waveform shape changed; build a new plan")
@@ -145,7 +185,7 @@ class FusedPlan:
 
     def refresh_medium(self):
         """Re-point the plan at the medium's buffers (after DeviceMedium.prepare)."""
-        _lib.check(self.lib.fdtd_plan_set_medium(self._plan, ptr(self.medium.coef),
+        _lib.check(self.lib.fdtd_plan_set_medium(self._plan, ptr(self.medium.coef), ptr(self.medium.diag),
                                                  ptr(self.medium.mur), ptr(self.waveforms)))
 
     def forward(self, traces=None, u_prev_out=None, u_out=None, save_checkpoints=False):
