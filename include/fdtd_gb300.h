@@ -45,12 +45,11 @@ enum {
 
 enum { FDTD_STORE_F32 = 0, FDTD_STORE_F16 = 1, FDTD_STORE_BF16 = 2 };
 
-/* Grid and medium. `coef`, `diag` and `mur` come from fdtd_prepare_medium. */
+/* Grid and medium. `coef` and `mur` come from fdtd_prepare_medium. */
 typedef struct fdtd_grid {
   int32_t ny, nx, pitch;
   double dx, dy, dt;
   const float* coef; /* device (ny, pitch): (c * dt)^2 */
-  const float* diag; /* device (ny, pitch): 2 - 2 (c * dt)^2 (1/dx^2 + 1/dy^2) */
   const float* mur;  /* device: k_left[ny], k_right[ny], k_bottom[nx], k_top[nx],
                         corner_kx[4], corner_ky[4] (corners in the order
                         (0,0), (0,nx-1), (ny-1,0), (ny-1,nx-1)) */
@@ -96,7 +95,8 @@ typedef struct fdtd_tuning {
   int32_t rows_per_lane;    /* rows each lane keeps in registers: 4 or 8 */
   int32_t warps;            /* warps per CTA (region height = warps * rows_per_lane) */
   int32_t steps_per_launch; /* leapfrog steps per HBM round trip (temporal block) */
-  int32_t ckpt_every;       /* checkpoint spacing in steps; 0 = about sqrt(2 nt) */
+  int32_t ckpt_every;       /* checkpoint spacing in steps, rounded up to a multiple of
+                               steps_per_launch; 0 = about sqrt(2 nt) */
   int32_t ckpt_store;       /* FDTD_STORE_F32 / _F16 / _BF16 */
   int32_t ctas_per_sm;      /* persistent grid = SMs * ctas_per_sm; 0 = 1 */
 } fdtd_tuning;
@@ -107,19 +107,18 @@ typedef struct fdtd_plan fdtd_plan; /* opaque host-side execution plan */
 int32_t fdtd_abi_version(void);
 const char* fdtd_last_error(void);
 
-/* Sound speed (device float64 (ny, nx), row stride nx) -> coef, diag and Mur
+/* Sound speed (device float64 (ny, nx), row stride nx) -> coef and Mur
    coefficients, computed in float64 and rounded to float32.
    Replaces TorchScalarWave2D.set_c (fdtd2d/torch_backend.py:158-168) and
    TorchFDTD2D._refresh_boundaries (fdtd2d/torch_backend.py:264-275). */
 int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pitch,
                             double dt, double dx, double dy,
-                            float* coef, float* diag, float* mur, void* stream);
+                            float* coef, float* mur, void* stream);
 
 /* ------------------------------------------------- one-step (plain) kernels */
 
 /* One leapfrog step for n_shots shots, Mur edges included:
      forward: u_next = 2u - u_old + coef * lap(u) + sources
-              (evaluated as diag * u - u_old + coef * (lap(u) - cdiag * u))
      adjoint: u_next = 2u - u_old + lap(coef * u) + sources
    Sources: `src_*` are device arrays of shape (n_shots, src_per_shot) (row, col,
    weight, waveform index) and inject w * waveforms[wave * waveform_len + step];
@@ -186,7 +185,7 @@ int32_t fdtd_plan_tuning(const fdtd_plan* plan, fdtd_tuning* tuning);
    tables into it; synchronises `stream` once. */
 int32_t fdtd_plan_bind(fdtd_plan* plan, void* workspace, size_t bytes, void* stream);
 /* Updates the medium and source waveform pointers of a bound plan (same shapes). */
-int32_t fdtd_plan_set_medium(fdtd_plan* plan, const float* coef, const float* diag, const float* mur,
+int32_t fdtd_plan_set_medium(fdtd_plan* plan, const float* coef, const float* mur,
                              const float* waveforms);
 
 /* Batched forward of every shot over n_steps with the fused temporally blocked

@@ -310,7 +310,7 @@ def residual_batch(predicted, observed, mute):
     return residual
 
 
-def adjoint_gradient_c2(c, dx, dy, dt, geo, wave, residual):
+def adjoint_gradient_c2(c, dx, dy, dt, geo, wave, residual, dtype=np.float64):
     """Summed-over-shots gradient with respect to c^2 by the reverse-time loop.
 
     Restates _adjoint_accumulate_batch with ``store_every = 1`` (invert_ring.py:
@@ -319,14 +319,18 @@ def adjoint_gradient_c2(c, dx, dy, dt, geo, wave, residual):
     scattered and injected, the adjoint field steps, and for n >= 1
     ``g += dt^2 * sum_shots(l+ * lap(wave[n-1]))`` with the zero-padded Laplacian.
     ``wave`` is ``(n_steps, S, ny, nx)``, ``residual`` ``(S, R, n_steps)``.
+    ``dtype`` float32 runs the fields in single precision (the reference's
+    float32 path) with the gradient still summed in float64.
     """
-    c = np.asarray(c, dtype=float)
+    c = np.asarray(c, dtype=dtype)
     c2 = c * c
-    dt2 = dt * dt
-    k = mur_coefficients(c, dt, dx, dy)
+    dt2 = dtype(dt) * dtype(dt)
+    k = mur_coefficients(c, dtype(dt), dtype(dx), dtype(dy))
     n_steps = residual.shape[2]
     n_shots = residual.shape[0]
-    l_old = np.zeros((n_shots,) + c.shape)
+    residual = np.asarray(residual, dtype=dtype)
+    geo = {key: (np.asarray(v, dtype=dtype) if key.startswith("w") else v) for key, v in geo.items()}
+    l_old = np.zeros((n_shots,) + c.shape, dtype=dtype)
     lam = np.zeros_like(l_old)
     g = np.zeros(c.shape)
     for n in range(n_steps - 1, -1, -1):
@@ -339,17 +343,19 @@ def adjoint_gradient_c2(c, dx, dy, dt, geo, wave, residual):
 
 
 def misfit_and_gradient_c2(c, dx, dy, dt, geo, source_fields, source_values, n_steps,
-                           observed, mute):
+                           observed, mute, dtype=np.float64):
     """Misfit ``0.5 * sum(residual^2)`` and the unmasked ``g_{c^2}``.
 
     The device part of TorchLeastSquaresFWI.misfit_and_grad (invert_ring.py:
-    634-656) for fixed shots with ``store_every = 1``, in float64.
+    634-656) for fixed shots with ``store_every = 1``, in ``dtype`` (float64 by
+    default).
     """
+    geo_d = {key: (np.asarray(v, dtype=dtype) if key.startswith("w") else v) for key, v in geo.items()}
     traces, _, _, wave = simulate_shots_batch(
-        c, dx, dy, dt, geo, source_fields, source_values, n_steps, store=True)
-    residual = residual_batch(traces, observed, mute)
-    misfit = 0.5 * float(np.sum(residual * residual))
-    return misfit, adjoint_gradient_c2(c, dx, dy, dt, geo, wave, residual)
+        c, dx, dy, dt, geo_d, source_fields, source_values, n_steps, store=True, dtype=dtype)
+    residual = residual_batch(traces, np.asarray(observed, dtype=dtype), mute)
+    misfit = 0.5 * float(np.sum(residual.astype(np.float64) ** 2))
+    return misfit, adjoint_gradient_c2(c, dx, dy, dt, geo, wave, residual, dtype=dtype)
 
 
 def gradient_m(g_c2, m, mask=None):

@@ -22,7 +22,7 @@ STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 class Grid(ctypes.Structure):
     _fields_ = [("ny", c_int32), ("nx", c_int32), ("pitch", c_int32),
                 ("dx", c_double), ("dy", c_double), ("dt", c_double),
-                ("coef", c_void_p), ("diag", c_void_p), ("mur", c_void_p)]
+                ("coef", c_void_p), ("mur", c_void_p)]
 
 
 class Receivers(ctypes.Structure):
@@ -52,7 +52,7 @@ _SIGNATURES = {
     "fdtd_abi_version": (c_int32, []),
     "fdtd_last_error": (ctypes.c_char_p, []),
     "fdtd_prepare_medium": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_double,
-                                      c_double, c_void_p, c_void_p, c_void_p, c_void_p]),
+                                      c_double, c_void_p, c_void_p, c_void_p]),
     "fdtd_step": (c_int32, [POINTER(Grid), c_int32, c_void_p, c_void_p, c_void_p, c_int32,
                             c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
                             c_void_p, c_int32, c_void_p]),
@@ -69,7 +69,7 @@ _SIGNATURES = {
     "fdtd_plan_workspace_bytes": (c_int32, [c_void_p, POINTER(c_size_t)]),
     "fdtd_plan_tuning": (c_int32, [c_void_p, POINTER(Tuning)]),
     "fdtd_plan_bind": (c_int32, [c_void_p, c_void_p, c_size_t, c_void_p]),
-    "fdtd_plan_set_medium": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fdtd_plan_set_medium": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "fdtd_forward": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
     "fdtd_adjoint": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "fdtd_residual_misfit": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int64,

@@ -26,11 +26,13 @@ __device__ __forceinline__ float lap5(float c, float l, float r, float d, float 
   return __fmaf_rn(c, cdiag, nbr4(l, r, d, u, idx2, idy2));
 }
 
-// Forward leapfrog u+ = 2u - u_old + (c dt)^2 lap(u) (fdtd2d/torch_backend.py:516),
-// regrouped as a u - u_old + (c dt)^2 nbr4 with the per-cell a = 2 + (c dt)^2 cdiag
-// precomputed in float64: two fused multiply-adds after nbr4.
-__device__ __forceinline__ float leap(float c, float p, float a, float coef, float nb) {
-  return __fmaf_rn(coef, nb, __fmaf_rn(a, c, -p));
+// Forward leapfrog u+ = 2u - u_old + (c dt)^2 lap(u) (fdtd2d/torch_backend.py:516).
+// 2u - u_old is formed with one rounding (2u is exact). The factor 2 must stay
+// exact: folding it into a per-cell 2 + (c dt)^2 cdiag rounded to float32 shifts
+// every mode's frequency by a fixed relative amount, which accumulates
+// coherently over thousands of steps.
+__device__ __forceinline__ float leap(float c, float p, float coef, float lap) {
+  return __fmaf_rn(coef, lap, __fmaf_rn(2.0f, c, -p));
 }
 
 // Adjoint leapfrog 2l - l_old + lap((c dt)^2 l)  (fdtd2d/torch_backend.py:531-532);
@@ -108,7 +110,6 @@ struct TbParams {
   int ny, nx, pitch;
   float idx2, idy2, cdiag;
   const float* coef;     // (c dt)^2
-  const float* diag;     // 2 + (c dt)^2 cdiag, forward update only
   const float* mur;
   // tiling
   const TbTile* tiles;
@@ -144,7 +145,7 @@ struct TbParams {
 // Dynamic shared-memory carve-up of the temporally blocked kernel; the host
 // sizes the launch with the same function.
 struct TbSmem {
-  size_t coef, diag, g, xch, tap, res, src, mask, base, srcpos, total;
+  size_t coef, g, xch, tap, res, src, mask, base, srcpos, total;
 };
 
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
@@ -155,7 +156,6 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
   const size_t region = size_t(nw) * ky * RX * sizeof(float);
   size_t off = 0;
   m.coef = off; off += region;
-  m.diag = off; if (mode != MODE_ADJ) off += region;
   m.g = off; if (mode == MODE_ADJ) off += region;
   m.xch = off; off += size_t(2) * nw * 2 * 32 * 16;
   m.tap = off; off += tb_align16(size_t(tmax) * (ntap_max > 0 ? ntap_max : 1) * sizeof(float));

@@ -23,7 +23,6 @@ struct StepArgs {
   int ny, nx, pitch;
   float idx2, idy2, cdiag;
   const float* coef;
-  const float* diag;
   const float* mur;
   int n_shots;
   const float* u_old;
@@ -51,7 +50,7 @@ cudaError_t image_launch(int ny, int nx, int pitch, float idx2, float idy2, floa
                          int n_shots, const float* adj, const float* fwd, double scale,
                          double* g, cudaStream_t st);
 cudaError_t prepare_medium_launch(const double* c, int ny, int nx, int pitch, double dt,
-                                  double dx, double dy, float* coef, float* diag, float* mur,
+                                  double dx, double dy, float* coef, float* mur,
                                   cudaStream_t st);
 cudaError_t residual_launch(int n_shots, int n_rx, int n_steps, const float* traces,
                             const float* observed, long long obs_shot_stride,

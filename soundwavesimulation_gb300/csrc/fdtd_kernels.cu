@@ -25,8 +25,8 @@ __device__ float cell_next(const StepArgs& a, int s, int y, int x) {
   const long long i = (long long)y * a.pitch + x;
   const float nb = nbr4(operand(a, u, y, x - 1), operand(a, u, y, x + 1), operand(a, u, y - 1, x),
                         operand(a, u, y + 1, x), a.idx2, a.idy2);
-  float un = a.adjoint ? leap_adj(u[i], uo[i], __fmaf_rn(operand(a, u, y, x), a.cdiag, nb))
-                       : leap(u[i], uo[i], a.diag[i], a.coef[i], nb);
+  const float lap = __fmaf_rn(operand(a, u, y, x), a.cdiag, nb);
+  float un = a.adjoint ? leap_adj(u[i], uo[i], lap) : leap(u[i], uo[i], a.coef[i], lap);
   if (a.src_per_shot > 0) {
     float acc = 0.f;
     bool hit = false;
@@ -137,19 +137,16 @@ __device__ __forceinline__ double mur_k(double c, double dt, double h) {
   return (c * dt - h) / (c * dt + h);
 }
 
-__global__ void coef_kernel(const double* c, int ny, int nx, int pitch, double dt, double cdiag,
-                            float* coef, float* diag) {
+__global__ void coef_kernel(const double* c, int ny, int nx, int pitch, double dt, float* coef) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= pitch || y >= ny) return;
-  float v = 0.f, d = 0.f;
+  float v = 0.f;
   if (x < nx) {
     const double cd = c[(long long)y * nx + x] * dt;
     v = (float)(cd * cd);
-    d = (float)(2.0 + cd * cd * cdiag);
   }
   coef[(long long)y * pitch + x] = v;
-  diag[(long long)y * pitch + x] = d;
 }
 
 __global__ void mur_kernel(const double* c, int ny, int nx, double dt, double dx, double dy,
@@ -301,12 +298,11 @@ cudaError_t image_launch(int ny, int nx, int pitch, float idx2, float idy2, floa
 }
 
 cudaError_t prepare_medium_launch(const double* c, int ny, int nx, int pitch, double dt,
-                                  double dx, double dy, float* coef, float* diag, float* mur,
+                                  double dx, double dy, float* coef, float* mur,
                                   cudaStream_t st) {
   dim3 block(32, 8);
   dim3 grid((pitch + 31) / 32, (ny + 7) / 8);
-  const double cdiag = -2.0 * (1.0 / (dx * dx) + 1.0 / (dy * dy));
-  coef_kernel<<<grid, block, 0, st>>>(c, ny, nx, pitch, dt, cdiag, coef, diag);
+  coef_kernel<<<grid, block, 0, st>>>(c, ny, nx, pitch, dt, coef);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int n = (ny > nx ? ny : nx);

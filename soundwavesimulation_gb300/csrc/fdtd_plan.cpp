@@ -129,7 +129,7 @@ int32_t validate_grid(const fdtd_grid& g) {
   if (g.ny < 8 || g.nx < 8) return fail(FDTD_ERR_INVALID, "grid must be at least 8 x 8");
   if (g.pitch < g.nx || g.pitch % 4 != 0) return fail(FDTD_ERR_INVALID, "pitch must be a multiple of 4 and >= nx");
   if (!(g.dx > 0) || !(g.dy > 0) || !(g.dt > 0)) return fail(FDTD_ERR_INVALID, "dx, dy and dt must be positive");
-  if (!g.coef || !g.diag || !g.mur) return fail(FDTD_ERR_INVALID, "coef, diag and mur must be set");
+  if (!g.coef || !g.mur) return fail(FDTD_ERR_INVALID, "coef and mur must be set");
   return FDTD_OK;
 }
 
@@ -144,7 +144,6 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.idy2 = (float)idy2;
   q.cdiag = (float)(-2.0 * (idx2 + idy2));
   q.coef = g.coef;
-  q.diag = g.diag;
   q.mur = g.mur;
   q.tiles = reinterpret_cast<const TbTile*>(p->ws + p->o_tiles);
   q.ntiles = (int)p->tiles.size();
@@ -403,11 +402,11 @@ int32_t fdtd_tap_table(int32_t ny, int32_t nx, const fdtd_receivers* rx, int32_t
 }
 
 int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pitch, double dt,
-                            double dx, double dy, float* coef, float* diag, float* mur, void* stream) {
-  if (!c || !coef || !diag || !mur) return fail(FDTD_ERR_INVALID, "null pointer");
+                            double dx, double dy, float* coef, float* mur, void* stream) {
+  if (!c || !coef || !mur) return fail(FDTD_ERR_INVALID, "null pointer");
   if (ny < 3 || nx < 3 || pitch < nx || pitch % 4) return fail(FDTD_ERR_INVALID, "bad grid shape");
   if (!(dt > 0) || !(dx > 0) || !(dy > 0)) return fail(FDTD_ERR_INVALID, "dt, dx and dy must be positive");
-  cudaError_t e = prepare_medium_launch(c, ny, nx, pitch, dt, dx, dy, coef, diag, mur, (cudaStream_t)stream);
+  cudaError_t e = prepare_medium_launch(c, ny, nx, pitch, dt, dx, dy, coef, mur, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "prepare_medium");
   return FDTD_OK;
 }
@@ -425,7 +424,6 @@ int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, co
   if (n_shots < 1) return fail(FDTD_ERR_INVALID, "n_shots must be positive");
   if (src_per_shot > 0 && (!src_row || !src_col || !src_w || !src_wave || !waveforms))
     return fail(FDTD_ERR_INVALID, "source arrays missing");
-  if (!adjoint && !grid->diag) return fail(FDTD_ERR_INVALID, "diag must be set for the forward step");
   StepArgs a;
   a.ny = grid->ny;
   a.nx = grid->nx;
@@ -435,7 +433,6 @@ int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, co
   a.idy2 = (float)idy2;
   a.cdiag = (float)(-2.0 * (idx2 + idy2));
   a.coef = grid->coef;
-  a.diag = grid->diag;
   a.mur = grid->mur;
   a.n_shots = n_shots;
   a.u_old = u_old;
@@ -566,7 +563,8 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
     const int c = (int)std::ceil(std::sqrt(2.0 * nt));
     t.ckpt_every = ((c + p->tmax - 1) / p->tmax) * p->tmax;
   }
-  if (t.ckpt_every % p->tmax) { delete p; return fail(FDTD_ERR_INVALID, "ckpt_every must be a multiple of steps_per_launch"); }
+  // checkpoints sit on temporal-block boundaries: round the spacing up to a multiple of T
+  t.ckpt_every = ((t.ckpt_every + p->tmax - 1) / p->tmax) * p->tmax;
   p->ckpt_every = t.ckpt_every;
   p->nseg = (nt + p->ckpt_every - 1) / p->ckpt_every;
   p->tun = t;
@@ -656,11 +654,10 @@ int32_t fdtd_plan_bind(fdtd_plan* p, void* workspace, size_t bytes, void* stream
   return FDTD_OK;
 }
 
-int32_t fdtd_plan_set_medium(fdtd_plan* p, const float* coef, const float* diag, const float* mur,
+int32_t fdtd_plan_set_medium(fdtd_plan* p, const float* coef, const float* mur,
                              const float* waveforms) {
   if (!p) return fail(FDTD_ERR_INVALID, "null plan");
   if (coef) p->prob.grid.coef = coef;
-  if (diag) p->prob.grid.diag = diag;
   if (mur) p->prob.grid.mur = mur;
   if (waveforms) p->prob.src.waveforms = waveforms;
   p->have_ckpt = false;

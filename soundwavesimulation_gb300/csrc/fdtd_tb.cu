@@ -39,7 +39,6 @@ struct Ctx {
   unsigned mask, srcsel;
   int base;
   float* s_coef;
-  float* s_diag;
   float* s_g;
   float4* s_xch;
   float* s_tap;
@@ -62,10 +61,12 @@ __device__ __forceinline__ float4 ldg4(const float* p) {
 
 // Mur edges and corners, in registers (plus shuffles across one lane boundary).
 // The tiler places rows 0/1 and ny-2/ny-1 in one band and column 0 at lane 0, c = 0.
-// Cells outside the domain need no treatment: their coef and diag are zero, so
-// in the forward they stay exactly zero (u+ = 0 * u - u_old + 0 starting from
-// zero), and in the adjoint their operand coef * l is zero, so whatever they
-// hold never reaches a domain cell and they are never written back.
+// Cells outside the domain need no per-step treatment: they are loaded as zero
+// and their coef is zero, so in the forward they stay exactly zero
+// (u+ = 2 * 0 - 0 + 0 * lap) and the zero-padded Laplacian
+// the recompute stores is exact; in the adjoint their operand coef * l is zero,
+// so whatever they hold never reaches a domain cell, and they are never written
+// back.
 template <int KY>
 __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY][4],
                                          const TbParams& p, const Ctx& x) {
@@ -189,7 +190,6 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   const float4* xin = x.s_xch + (k & 1) * x.nw * 64;
   float4* xout = x.s_xch + ((k + 1) & 1) * x.nw * 64;
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
-  const float4* diag4 = reinterpret_cast<const float4*>(x.s_diag) + (x.w * KY) * 32 + x.lane;
   const float idx2 = p.idx2, idy2 = p.idy2, cdiag = p.cdiag;
 
   // ---- stencil over the band, rolling the row above / below
@@ -221,10 +221,9 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
       P[r][3] = leap_adj(C[r][3], P[r][3], __fmaf_rn(cur.w, cdiag, n3));
     } else {
       const float4 co = coef4[r * 32];
-      const float4 dg = diag4[r * 32];
+      const float l0 = __fmaf_rn(cur.x, cdiag, n0), l1 = __fmaf_rn(cur.y, cdiag, n1);
+      const float l2 = __fmaf_rn(cur.z, cdiag, n2), l3 = __fmaf_rn(cur.w, cdiag, n3);
       if (MODE == MODE_REC && ((x.own_rows >> r) & 1u)) {
-        const float l0 = __fmaf_rn(cur.x, cdiag, n0), l1 = __fmaf_rn(cur.y, cdiag, n1);
-        const float l2 = __fmaf_rn(cur.z, cdiag, n2), l3 = __fmaf_rn(cur.w, cdiag, n3);
         float* dst = segrow + (long long)r * p.pitch;
         if (x.own_cols == 0xFu) {
           *reinterpret_cast<float4*>(dst) = make_float4(l0, l1, l2, l3);
@@ -235,10 +234,10 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
           if (x.own_cols & 8u) dst[3] = l3;
         }
       }
-      P[r][0] = leap(C[r][0], P[r][0], dg.x, co.x, n0);
-      P[r][1] = leap(C[r][1], P[r][1], dg.y, co.y, n1);
-      P[r][2] = leap(C[r][2], P[r][2], dg.z, co.z, n2);
-      P[r][3] = leap(C[r][3], P[r][3], dg.w, co.w, n3);
+      P[r][0] = leap(C[r][0], P[r][0], co.x, l0);
+      P[r][1] = leap(C[r][1], P[r][1], co.y, l1);
+      P[r][2] = leap(C[r][2], P[r][2], co.z, l2);
+      P[r][3] = leap(C[r][3], P[r][3], co.w, l3);
     }
     prv = cur;
     cur = nxt;
@@ -357,6 +356,13 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
     }
     P[r][0] = a.x; P[r][1] = a.y; P[r][2] = a.z; P[r][3] = a.w;
     C[r][0] = b.x; C[r][1] = b.y; C[r][2] = b.z; C[r][3] = b.w;
+    if (EDGE) {
+      // padding columns start at zero whatever the buffer holds there
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (x.xb + c >= p.nx) { P[r][c] = 0.f; C[r][c] = 0.f; }
+      }
+    }
   }
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
   x.s_xch[x.w * 64 + x.lane] = opval<MODE>(C[0], coef4[0]);
@@ -386,7 +392,6 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
   x.lane = x.tid & 31;
   x.nw = nw;
   x.s_coef = reinterpret_cast<float*>(smem + L.coef);
-  x.s_diag = reinterpret_cast<float*>(smem + L.diag);
   x.s_g = reinterpret_cast<float*>(smem + L.g);
   x.s_xch = reinterpret_cast<float4*>(smem + L.xch);
   x.s_tap = reinterpret_cast<float*>(smem + L.tap);
@@ -427,19 +432,14 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
       const int yy = x.y0 + r;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f), d = v;
-      if (yy >= 0 && yy < p.ny && x.xb < p.pitch) {
-        v = ldg4(p.coef + (long long)yy * p.pitch + x.xb);
-        if (MODE != MODE_ADJ) d = ldg4(p.diag + (long long)yy * p.pitch + x.xb);
-      }
-      if (x.xb + 0 >= p.nx) { v.x = 0.f; d.x = 0.f; }
-      if (x.xb + 1 >= p.nx) { v.y = 0.f; d.y = 0.f; }
-      if (x.xb + 2 >= p.nx) { v.z = 0.f; d.z = 0.f; }
-      if (x.xb + 3 >= p.nx) { v.w = 0.f; d.w = 0.f; }
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (yy >= 0 && yy < p.ny && x.xb < p.pitch) v = ldg4(p.coef + (long long)yy * p.pitch + x.xb);
+      if (x.xb + 0 >= p.nx) v.x = 0.f;
+      if (x.xb + 1 >= p.nx) v.y = 0.f;
+      if (x.xb + 2 >= p.nx) v.z = 0.f;
+      if (x.xb + 3 >= p.nx) v.w = 0.f;
       reinterpret_cast<float4*>(x.s_coef)[(x.w * KY + r) * 32 + x.lane] = v;
-      if (MODE != MODE_ADJ) {
-        reinterpret_cast<float4*>(x.s_diag)[(x.w * KY + r) * 32 + x.lane] = d;
-      } else {
+      if (MODE == MODE_ADJ) {
         reinterpret_cast<float4*>(x.s_g)[(x.w * KY + r) * 32 + x.lane] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }

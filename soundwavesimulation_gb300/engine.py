@@ -57,7 +57,6 @@ class DeviceMedium:
         self.dx, self.dy, self.dt = float(dx), float(dy), float(dt)
         self.c64 = c64
         self.coef = torch.zeros((self.ny, self.pitch), dtype=torch.float32, device=self.device)
-        self.diag = torch.zeros((self.ny, self.pitch), dtype=torch.float32, device=self.device)
         self.mur = torch.zeros(2 * self.ny + 2 * self.nx + 8, dtype=torch.float32, device=self.device)
         self.prepare()
 
@@ -75,12 +74,12 @@ class DeviceMedium:
     def prepare(self):
         lib = _lib.load()
         _lib.check(lib.fdtd_prepare_medium(ptr(self.c64), self.ny, self.nx, self.pitch, self.dt,
-                                           self.dx, self.dy, ptr(self.coef), ptr(self.diag),
-                                           ptr(self.mur), stream_handle(self.device)), "prepare_medium")
+                                           self.dx, self.dy, ptr(self.coef), ptr(self.mur),
+                                           stream_handle(self.device)), "prepare_medium")
 
     def grid(self) -> _lib.Grid:
         return _lib.Grid(self.ny, self.nx, self.pitch, self.dx, self.dy, self.dt,
-                         ptr(self.coef), ptr(self.diag), ptr(self.mur))
+                         ptr(self.coef), ptr(self.mur))
 
     def new_field(self, n_shots=None):
         shape = (self.ny, self.pitch) if n_shots is None else (int(n_shots), self.ny, self.pitch)
@@ -185,8 +184,8 @@ class FusedPlan(ProblemTables):
 
     def refresh_medium(self):
         """Re-point the plan at the medium's buffers (after DeviceMedium.prepare)."""
-        _lib.check(self.lib.fdtd_plan_set_medium(self._plan, ptr(self.medium.coef), ptr(self.medium.diag),
-                                                 ptr(self.medium.mur), ptr(self.waveforms)))
+        _lib.check(self.lib.fdtd_plan_set_medium(self._plan, ptr(self.medium.coef), ptr(self.medium.mur),
+                                                 ptr(self.waveforms)))
 
     def forward(self, traces=None, u_prev_out=None, u_out=None, save_checkpoints=False):
         """Run all shots for n_steps; returns traces (S, R, nt) float32."""

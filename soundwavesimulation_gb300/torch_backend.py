@@ -299,7 +299,7 @@ class TorchRingSampler:
         return self.row0, self.col0, self.weights
 
     def _grid(self, pitch):
-        return _lib.Grid(self.grid_shape[0], self.grid_shape[1], int(pitch), 1.0, 1.0, 1.0, 0, 0, 0)
+        return _lib.Grid(self.grid_shape[0], self.grid_shape[1], int(pitch), 1.0, 1.0, 1.0, 0, 0)
 
     def _gather(self, fields, n_shots):
         if fields.dtype != torch.float32 or fields.stride(-1) != 1 or fields.device != self.device:
