@@ -242,6 +242,23 @@ int32_t fdtd_gradient_plain(const fdtd_problem* problem, const float* observed,
                             void* workspace, size_t bytes, void* stream);
 size_t fdtd_gradient_plain_workspace(const fdtd_problem* problem);
 
+/* Size of the fixed device scratch behind fdtd_forward_plain_static: three
+   fields of one shot plus the receiver and source tables must fit (about
+   1180 x 1180 cells at most; 1024 x 1024 with 512 receivers uses ~12 MiB). */
+#define FDTD_STATIC_SCRATCH_BYTES (16u << 20)
+
+/* fdtd_forward_plain for callers that cannot allocate device memory (no
+   counterpart in the reference). Same problem and traces as
+   fdtd_forward_plain, no workspace: the scratch is a file-scope device array of
+   FDTD_STATIC_SCRATCH_BYTES that every GPU loading the library holds until exit.
+   Calls no cudaMalloc, cudaFree or allocating library routine. Problems that do
+   not fit return FDTD_ERR_WORKSPACE with a message. The first call on a device
+   looks up the array's address (cudaGetSymbolAddress, that device current) and
+   caches it: make that first call before any stream capture. All calls share
+   the array and it keeps the last call's contents (each shot clears the fields
+   it uses); calls that overlap on the GPU race on it. */
+int32_t fdtd_forward_plain_static(const fdtd_problem* problem, float* traces, void* stream);
+
 /* ------------------------------------------------------- tiling (host) */
 
 /* The 1-D tiler of the fused engine, exposed for tests: covers [0, n) with

@@ -80,6 +80,7 @@ _SIGNATURES = {
     "fdtd_gradient_plain": (c_int32, [POINTER(Problem), c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_size_t, c_void_p]),
     "fdtd_gradient_plain_workspace": (c_size_t, [POINTER(Problem)]),
+    "fdtd_forward_plain_static": (c_int32, [POINTER(Problem), c_void_p, c_void_p]),
     "fdtd_tile_axis": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32, c_int32,
                                  c_void_p, POINTER(c_int32)]),
 }
