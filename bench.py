@@ -149,6 +149,111 @@ def run_reference(args):
     return 0
 
 
+def bench_gradient(args, acq, medium, rx, waves, observed, tuning, device, world, barrier,
+                   solver, sampler, observed_nearest):
+    """FWI gradient at the workload's grid and shots; returns the JSON object."""
+    import torch
+    from soundwavesimulation_gb300 import fwi, interior_mask
+    from soundwavesimulation_gb300.engine import (DeviceMedium, FusedPlan, ProblemTables, gradient_plain,
+                                                  residual_misfit)
+    from soundwavesimulation_gb300.phantoms import blurred_start
+    from soundwavesimulation_gb300.sharding import allreduce_misfit_and_gradient
+    n, nt, S = acq.n, acq.n_steps, acq.n_shots
+    mask = interior_mask(acq.x, acq.x, 0.45 * n * acq.dx, margin_m=3 * acq.dx)
+    c_start = blurred_start(acq.c, 10.0, mask)
+    start = DeviceMedium(c_start, acq.dx, acq.dx, acq.dt, device)
+    plan = FusedPlan(start, rx, acq.source_tables(), waves, nt, tuning=tuning, for_gradient=True)
+    mute = torch.as_tensor(acq.tx, dtype=torch.int32, device=device)
+    g = torch.zeros((n, start.pitch), dtype=torch.float64, device=device)
+    misfit = torch.zeros(1, dtype=torch.float64, device=device)
+    work = torch.empty_like(observed)
+
+    def step():
+        g.zero_()
+        misfit.zero_()
+        tr = plan.forward(work, save_checkpoints=True)
+        residual_misfit(tr, observed, mute, residual=tr, misfit=misfit)
+        plan.adjoint(tr, g)
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    for k in range(args.steps):
+        step()
+        ev[k + 1].record(stream)
+    barrier()
+    ms = float(np.mean([ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]))
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        allreduce_misfit_and_gradient(misfit, g)
+    value = acq.cell_updates * world / (ms * 1e-3) / 1e9
+    launches = sum(1 for _ in range(0, nt, plan.tuning["steps_per_launch"]))
+
+    # plain per-shot gradient (full history, one launch per kernel per step) on one shot
+    one = acq.subset(n_shots=1)
+    tables = ProblemTables(start, rx, one.source_tables(), waves, nt)
+    gradient_plain(tables, observed[:1], mute[:1])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    Jp, gp = gradient_plain(tables, observed[:1], mute[:1])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    plain_value = float(n) ** 2 * nt / (plain_ms * 1e-3) / 1e9
+    # the fused gradient of that one shot, for an agreement figure
+    p1 = FusedPlan(start, rx, one.source_tables(), waves, nt, tuning=tuning, for_gradient=True)
+    tr1 = p1.forward(save_checkpoints=True)
+    J1 = torch.zeros(1, dtype=torch.float64, device=device)
+    residual_misfit(tr1, observed[:1], mute[:1], residual=tr1, misfit=J1)
+    g1 = torch.zeros_like(g)
+    p1.adjoint(tr1, g1)
+    agree = float(torch.linalg.vector_norm(g1 - gp) / torch.linalg.vector_norm(gp))
+    del p1, tr1
+
+    # end to end through the public API: host slowness in, host gradient out
+    problem = fwi.TorchLeastSquaresFWI(solver, sampler, acq.ring, acq.wavelet, nt, acq.n_elements,
+                                       _full_gather(observed_nearest, acq), mask, parallel_shots=S,
+                                       tuning=tuning)
+    m_host = 1.0 / c_start ** 2
+    problem.gradient_c2(m_host, acq.tx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e_steps = max(1, min(args.steps, 2))
+    for _ in range(e_steps):
+        problem.gradient_c2(m_host, acq.tx)
+    e2e_s = (time.perf_counter() - t0) / e_steps
+    hbm, peak_kind = peaks()
+    achieved = GRAD_BYTES_PER_CELL * acq.cell_updates / (ms * 1e-3) / 1e9
+    return {
+        "value": value, "unit": UNIT, "ms_per_step": ms, "metric": "FWI gradient shot-cell-step updates/s",
+        "workload": f"{n}x{n}, {S} shots, {nt} steps, blurred (sigma 10 cells) start, checkpoints every "
+                    f"{plan.tuning['ckpt_every']} steps (float32)",
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "note": f"28 B per shot-cell-step algorithmic; peak {peak_kind}"},
+        "plain": {"value": plain_value, "unit": UNIT, "shots_sampled": 1, "speedup": value / world / plain_value,
+                  "rel_l2_fused_vs_plain": agree},
+        "e2e": {"value": acq.cell_updates * world / e2e_s / 1e9, "unit": UNIT,
+                "h2d_bytes_per_step": int(m_host.size * 8), "d2h_bytes_per_step": int(n * n * 8)},
+        "gpu_launches_per_step": 3 * launches + 2,
+        "workspace_gib": plan.workspace_bytes / 2 ** 30,
+    }
+
+
+def _full_gather(traces, acq):
+    """(n_elements, R, nt) observed gathers with the bench's shots at their transmitter rows."""
+    import torch
+    full = torch.zeros((acq.n_elements,) + tuple(traces.shape[1:]), dtype=torch.float32, device=traces.device)
+    full[torch.as_tensor(acq.tx, device=traces.device)] = traces
+    return full
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -239,6 +344,10 @@ def run_ours(args):
     h2d = acq.c.size * 8 + nt * 4 + 2 * S * 8
     d2h = int(host_traces.numel()) * 4
 
+    # ---- FWI gradient, same grid and shots: forward with checkpoints + residual + adjoint
+    grad = bench_gradient(args, acq, medium, rx, waves, traces, tuning, device, world, barrier,
+                          solver, sampler, tr)
+
     hbm, peak_kind = peaks()
     achieved = FWD_BYTES_PER_CELL * acq.cell_updates / (ms * 1e-3) / 1e9
     out = None
@@ -261,6 +370,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": d2h},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port", "sample": cpu_s},
+            "grad": grad,
             "gpu_launches": launches_per_pass * args.steps,
             "clocks": clocks.summary(),
             "wall_s": wall,
