@@ -145,7 +145,7 @@ struct TbParams {
 // Dynamic shared-memory carve-up of the temporally blocked kernel; the host
 // sizes the launch with the same function.
 struct TbSmem {
-  size_t coef, g, xch, tap, res, src, mask, base, srcpos, total;
+  size_t coef, lap, g, xch, tap, res, src, mask, base, srcpos, total;
 };
 
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
@@ -155,7 +155,12 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
   TbSmem m;
   const size_t region = size_t(nw) * ky * RX * sizeof(float);
   size_t off = 0;
-  m.coef = off; off += region;
+  // forward / recompute keep the region's coefficients in shared memory; the
+  // adjoint reads them through L1 and uses the space to stream in the next
+  // step's Laplacian tile (cp.async) instead
+  m.coef = off;
+  m.lap = off;
+  off += region;
   m.g = off; if (mode == MODE_ADJ) off += region;
   m.xch = off; off += size_t(2) * nw * 2 * 32 * 16;
   m.tap = off; off += tb_align16(size_t(tmax) * (ntap_max > 0 ? ntap_max : 1) * sizeof(float));

@@ -37,8 +37,11 @@ struct Ctx {
   int y0, xb;               // global row of this thread's r = 0, column of c = 0
   unsigned own_rows, own_cols;
   unsigned mask, srcsel;
+  unsigned rowvalid;        // band rows inside the domain (adjoint coefficient loads)
   int base;
+  const float* gcoef;       // global coefficients at (y0, xb) (adjoint)
   float* s_coef;
+  float* s_lap;
   float* s_g;
   float4* s_xch;
   float* s_tap;
@@ -57,6 +60,53 @@ __device__ __forceinline__ float4 opval(const float (&v)[4], float4 co) {
 
 __device__ __forceinline__ float4 ldg4(const float* p) {
   return __ldg(reinterpret_cast<const float4*>(p));
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Coefficients (c dt)^2 of band row r: from the shared-memory copy of the region
+// (forward, recompute) or through L1 from global memory (adjoint); zero outside
+// the domain.
+template <int MODE>
+__device__ __forceinline__ float4 coefrow(const TbParams& p, const Ctx& x, const float4* coef4, int r) {
+  if (MODE != MODE_ADJ) return coef4[r * 32];
+  if (!((x.rowvalid >> r) & 1u)) return make_float4(0.f, 0.f, 0.f, 0.f);
+  return ldg4(x.gcoef + (long long)r * p.pitch);
+}
+
+// Streams lap(u^{n-1}) of this thread's owned cells for adjoint step n into its
+// slots of the shared-memory Laplacian tile.
+template <int KY>
+__device__ __forceinline__ void prefetch_lap(const TbParams& p, const Ctx& x, int n) {
+  const float* sl = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
+                    ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
+  float* dst = x.s_lap + (x.w * KY) * RX + 4 * x.lane;
+#pragma unroll
+  for (int r = 0; r < KY; ++r) {
+    if ((x.own_rows >> r) & 1u) {
+      if (x.own_cols == 0xFu) {
+        cp_async16(dst + r * RX, sl + (long long)r * p.pitch);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if ((x.own_cols >> c) & 1u) cp_async4(dst + r * RX + c, sl + (long long)r * p.pitch + c);
+        }
+      }
+    }
+  }
+  cp_async_commit();
 }
 
 // Mur edges and corners, in registers (plus shuffles across one lane boundary).
@@ -195,7 +245,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   // ---- stencil over the band, rolling the row above / below
   float4 prv = (x.w > 0) ? xin[(x.w - 1) * 64 + 32 + x.lane] : zero4;
   const float4 below = (x.w < x.nw - 1) ? xin[(x.w + 1) * 64 + x.lane] : zero4;
-  float4 cur = opval<MODE>(C[0], coef4[0]);
+  float4 cur = opval<MODE>(C[0], coefrow<MODE>(p, x, coef4, 0));
   const bool lzero = EDGE && x.lane == 0 && x.rx0 == 0;
   const bool rzero = EDGE && x.lane == 31 && (x.rx0 + RX >= p.nx);
   float* segrow = nullptr;
@@ -205,7 +255,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
 #pragma unroll
   for (int r = 0; r < KY; ++r) {
-    const float4 nxt = (r + 1 < KY) ? opval<MODE>(C[r + 1], coef4[(r + 1) * 32]) : below;
+    const float4 nxt = (r + 1 < KY) ? opval<MODE>(C[r + 1], coefrow<MODE>(p, x, coef4, r + 1)) : below;
     float lft = __shfl_up_sync(FULL, cur.w, 1);
     float rgt = __shfl_down_sync(FULL, cur.x, 1);
     if (lzero) lft = 0.f;
@@ -283,36 +333,32 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
       }
     }
   }
-  if (MODE == MODE_ADJ && n >= 1 && x.own_rows && x.own_cols) {
-    const float* sl = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
-                      ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
-    float4* g4 = reinterpret_cast<float4*>(x.s_g) + (x.w * KY) * 32 + x.lane;
+  if (MODE == MODE_ADJ && x.own_rows && x.own_cols) {
+    if (n >= 1) {
+      // lap(u^{n-1}) of this thread's owned cells was streamed into shared
+      // memory (cp.async) during the previous step
+      cp_async_wait_all();
+      const float4* l4 = reinterpret_cast<const float4*>(x.s_lap) + (x.w * KY) * 32 + x.lane;
+      float4* g4 = reinterpret_cast<float4*>(x.s_g) + (x.w * KY) * 32 + x.lane;
 #pragma unroll
-    for (int r = 0; r < KY; ++r) {
-      if ((x.own_rows >> r) & 1u) {
-        float4 lv;
-        if (x.own_cols == 0xFu) {
-          lv = ldg4(sl + (long long)r * p.pitch);
-        } else {
-          const float* q = sl + (long long)r * p.pitch;
-          lv.x = (x.own_cols & 1u) ? __ldg(q + 0) : 0.f;
-          lv.y = (x.own_cols & 2u) ? __ldg(q + 1) : 0.f;
-          lv.z = (x.own_cols & 4u) ? __ldg(q + 2) : 0.f;
-          lv.w = (x.own_cols & 8u) ? __ldg(q + 3) : 0.f;
+      for (int r = 0; r < KY; ++r) {
+        if ((x.own_rows >> r) & 1u) {
+          const float4 lv = l4[r * 32];
+          float4 gv = g4[r * 32];
+          if (x.own_cols & 1u) gv.x = __fmaf_rn(P[r][0], lv.x, gv.x);
+          if (x.own_cols & 2u) gv.y = __fmaf_rn(P[r][1], lv.y, gv.y);
+          if (x.own_cols & 4u) gv.z = __fmaf_rn(P[r][2], lv.z, gv.z);
+          if (x.own_cols & 8u) gv.w = __fmaf_rn(P[r][3], lv.w, gv.w);
+          g4[r * 32] = gv;
         }
-        float4 gv = g4[r * 32];
-        if (x.own_cols & 1u) gv.x = __fmaf_rn(P[r][0], lv.x, gv.x);
-        if (x.own_cols & 2u) gv.y = __fmaf_rn(P[r][1], lv.y, gv.y);
-        if (x.own_cols & 4u) gv.z = __fmaf_rn(P[r][2], lv.z, gv.z);
-        if (x.own_cols & 8u) gv.w = __fmaf_rn(P[r][3], lv.w, gv.w);
-        g4[r * 32] = gv;
       }
     }
+    if (k + 1 < p.nsteps && n - 1 >= 1) prefetch_lap<KY>(p, x, n - 1);
   }
 
   // ---- publish the band's first and last rows for the next step
-  xout[x.w * 64 + x.lane] = opval<MODE>(P[0], coef4[0]);
-  xout[x.w * 64 + 32 + x.lane] = opval<MODE>(P[KY - 1], coef4[(KY - 1) * 32]);
+  xout[x.w * 64 + x.lane] = opval<MODE>(P[0], coefrow<MODE>(p, x, coef4, 0));
+  xout[x.w * 64 + 32 + x.lane] = opval<MODE>(P[KY - 1], coefrow<MODE>(p, x, coef4, KY - 1));
   __syncthreads();
 }
 
@@ -365,8 +411,9 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
     }
   }
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
-  x.s_xch[x.w * 64 + x.lane] = opval<MODE>(C[0], coef4[0]);
-  x.s_xch[x.w * 64 + 32 + x.lane] = opval<MODE>(C[KY - 1], coef4[(KY - 1) * 32]);
+  x.s_xch[x.w * 64 + x.lane] = opval<MODE>(C[0], coefrow<MODE>(p, x, coef4, 0));
+  x.s_xch[x.w * 64 + 32 + x.lane] = opval<MODE>(C[KY - 1], coefrow<MODE>(p, x, coef4, KY - 1));
+  if (MODE == MODE_ADJ && x.own_rows && x.own_cols && p.n0 >= 1) prefetch_lap<KY>(p, x, p.n0);
   __syncthreads();
 
   for (int k = 0; k < p.nsteps; k += 2) {
@@ -392,6 +439,7 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
   x.lane = x.tid & 31;
   x.nw = nw;
   x.s_coef = reinterpret_cast<float*>(smem + L.coef);
+  x.s_lap = reinterpret_cast<float*>(smem + L.lap);
   x.s_g = reinterpret_cast<float*>(smem + L.g);
   x.s_xch = reinterpret_cast<float4*>(smem + L.xch);
   x.s_tap = reinterpret_cast<float*>(smem + L.tap);
@@ -416,11 +464,14 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
     x.y0 = t.ry0 + x.w * KY;
     x.xb = t.rx0 + 4 * x.lane;
     x.own_rows = 0;
+    x.rowvalid = 0;
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
       const int yy = x.y0 + r;
       if (yy >= t.oy0 && yy < t.oy1) x.own_rows |= 1u << r;
+      if (yy >= 0 && yy < p.ny && x.xb < p.pitch) x.rowvalid |= 1u << r;
     }
+    x.gcoef = p.coef + (long long)x.y0 * p.pitch + x.xb;
     x.own_cols = 0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -428,18 +479,15 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
       if (xx >= t.ox0 && xx < t.ox1) x.own_cols |= 1u << c;
     }
 
-    // coefficients of the region (zero outside the domain)
+    // coefficients of the region (zero outside the domain; the padding columns of
+    // coef are zero in memory) or, for the adjoint, a cleared gradient tile
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
-      const int yy = x.y0 + r;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (yy >= 0 && yy < p.ny && x.xb < p.pitch) v = ldg4(p.coef + (long long)yy * p.pitch + x.xb);
-      if (x.xb + 0 >= p.nx) v.x = 0.f;
-      if (x.xb + 1 >= p.nx) v.y = 0.f;
-      if (x.xb + 2 >= p.nx) v.z = 0.f;
-      if (x.xb + 3 >= p.nx) v.w = 0.f;
-      reinterpret_cast<float4*>(x.s_coef)[(x.w * KY + r) * 32 + x.lane] = v;
-      if (MODE == MODE_ADJ) {
+      if (MODE != MODE_ADJ) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if ((x.rowvalid >> r) & 1u) v = ldg4(x.gcoef + (long long)r * p.pitch);
+        reinterpret_cast<float4*>(x.s_coef)[(x.w * KY + r) * 32 + x.lane] = v;
+      } else {
         reinterpret_cast<float4*>(x.s_g)[(x.w * KY + r) * 32 + x.lane] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
