@@ -273,7 +273,13 @@ def run_ours(args):
     medium = DeviceMedium(acq.c, acq.dx, acq.dx, acq.dt, device)
     rx = acq.ring.receiver_taps()
     waves = torch.as_tensor(acq.wavelet[None], dtype=torch.float32, device=device)
-    tuning = tb.engine_tuning()
+    if args.tuning:
+        tuning = json.loads(args.tuning)
+    else:
+        from soundwavesimulation_gb300.autotune import autotune
+        t_tune = time.perf_counter()
+        tuning = autotune(medium, rx, acq.source_tables(), waves, nt, verbose=rank == 0)
+        print(f"autotune {time.perf_counter() - t_tune:.1f} s -> {tuning}", file=sys.stderr)
     plan = FusedPlan(medium, rx, acq.source_tables(), waves, nt, tuning=tuning)
     traces = torch.empty((S, acq.n_elements, nt), dtype=torch.float32, device=device)
     launches_per_pass = math.ceil(nt / plan.tuning["steps_per_launch"])

@@ -427,8 +427,8 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
   }
 }
 
-template <int KY, int MODE>
-__global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbParams p) {
+template <int KY, int MODE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = p.nwarps;
   const int nthr = nw * 32;
@@ -595,30 +595,36 @@ __global__ void __launch_bounds__(KY == 8 ? 512 : 1024, 1) tb_kernel(const TbPar
   }
 }
 
-template <int KY, int MODE>
+template <int KY, int MODE, int MAXT>
 cudaError_t launch_one(const TbParams& p, int grid, size_t smem, cudaStream_t st) {
   static size_t configured_smem = 0;
   if (smem > configured_smem) {
-    cudaError_t e = cudaFuncSetAttribute(tb_kernel<KY, MODE>,
+    cudaError_t e = cudaFuncSetAttribute(tb_kernel<KY, MODE, MAXT>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured_smem = smem;
   }
-  tb_kernel<KY, MODE><<<grid, p.nwarps * 32, smem, st>>>(p);
+  tb_kernel<KY, MODE, MAXT><<<grid, p.nwarps * 32, smem, st>>>(p);
   return cudaGetLastError();
+}
+
+template <int KY, int MAXT>
+cudaError_t launch_mode(const TbParams& p, int mode, int grid, size_t smem, cudaStream_t st) {
+  if (mode == MODE_FWD) return launch_one<KY, MODE_FWD, MAXT>(p, grid, smem, st);
+  if (mode == MODE_REC) return launch_one<KY, MODE_REC, MAXT>(p, grid, smem, st);
+  return launch_one<KY, MODE_ADJ, MAXT>(p, grid, smem, st);
 }
 
 }  // namespace
 
+// Instantiations: KY = 8 rows per lane with at most 12 warps (168 registers per
+// thread, no spills) or 16 warps (128 registers); KY = 4 with at most 16 warps.
 cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st) {
   if (ky == 8) {
-    if (mode == MODE_FWD) return launch_one<8, MODE_FWD>(p, grid, smem, st);
-    if (mode == MODE_REC) return launch_one<8, MODE_REC>(p, grid, smem, st);
-    return launch_one<8, MODE_ADJ>(p, grid, smem, st);
+    if (p.nwarps <= 12) return launch_mode<8, 384>(p, mode, grid, smem, st);
+    return launch_mode<8, 512>(p, mode, grid, smem, st);
   }
-  if (mode == MODE_FWD) return launch_one<4, MODE_FWD>(p, grid, smem, st);
-  if (mode == MODE_REC) return launch_one<4, MODE_REC>(p, grid, smem, st);
-  return launch_one<4, MODE_ADJ>(p, grid, smem, st);
+  return launch_mode<4, 512>(p, mode, grid, smem, st);
 }
 
 }  // namespace fdtd
