@@ -405,13 +405,23 @@ def run_profile(args):
     tuning = json.loads(args.tuning) if args.tuning else {}
     plan = FusedPlan(medium, acq.ring.receiver_taps(), acq.source_tables(), waves, acq.n_steps,
                      tuning=tuning, for_gradient=args.profile == "grad")
-    traces = plan.forward(save_checkpoints=args.profile == "grad")
-    if args.profile == "grad":
-        res, _ = residual_misfit(traces, torch.zeros_like(traces), None)
-        g = torch.zeros((medium.ny, medium.pitch), dtype=torch.float64, device=device)
-        plan.adjoint(res, g)
-    torch.cuda.synchronize()
-    print(f"profile {args.profile}: {acq.n_shots} shots, {acq.n_steps} steps, tuning {plan.tuning}")
+    grad = args.profile == "grad"
+    times = []
+    for _ in range(2):  # the second pass is timed
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        traces = plan.forward(save_checkpoints=grad)
+        ev[1].record()
+        if grad:
+            res, _ = residual_misfit(traces, torch.zeros_like(traces), None)
+            g = torch.zeros((medium.ny, medium.pitch), dtype=torch.float64, device=device)
+            plan.adjoint(res, g)
+        ev[2].record()
+        torch.cuda.synchronize()
+        times = [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])]
+    print(f"profile {args.profile}: {acq.n_shots} shots, {acq.n_steps} steps, tuning {plan.tuning}; "
+          f"forward {times[0]:.2f} ms" + (f", residual+adjoint {times[1]:.2f} ms" if grad else ""))
     return 0
 
 

@@ -50,9 +50,11 @@ typedef struct fdtd_grid {
   int32_t ny, nx, pitch;
   double dx, dy, dt;
   const float* coef; /* device (ny, pitch): (c * dt)^2 */
-  const float* mur;  /* device: k_left[ny], k_right[ny], k_bottom[nx], k_top[nx],
-                        corner_kx[4], corner_ky[4] (corners in the order
-                        (0,0), (0,nx-1), (ny-1,0), (ny-1,nx-1)) */
+  const float* mur;  /* device, 2 * (2 ny + 2 nx + 8) floats: k_left[ny], k_right[ny],
+                        k_bottom[nx], k_top[nx], corner_kx[4], corner_ky[4] (corners
+                        in the order (0,0), (0,nx-1), (ny-1,0), (ny-1,nx-1)), then in
+                        the same layout the ratios coef_edge / coef_inner used by the
+                        adjoint in w = coef * l form */
 } fdtd_grid;
 
 /* Bilinear receivers (host arrays of length n). Receiver i samples rows
@@ -119,7 +121,10 @@ int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pit
 
 /* One leapfrog step for n_shots shots, Mur edges included:
      forward: u_next = 2u - u_old + coef * lap(u) + sources
-     adjoint: u_next = 2u - u_old + lap(coef * u) + sources
+     adjoint = 1: u_next = 2u - u_old + lap(coef * u) + sources
+     adjoint = 2: the same adjoint carried as w = coef * u:
+                  w_next = 2w - w_old + coef * lap(w) + coef * sources, with the
+                  Mur edges rescaled by the coef ratios (the fused engine's form)
    Sources: `src_*` are device arrays of shape (n_shots, src_per_shot) (row, col,
    weight, waveform index) and inject w * waveforms[wave * waveform_len + step];
    `dense` (device (n_shots, ny, pitch), nullable) is added as a field.

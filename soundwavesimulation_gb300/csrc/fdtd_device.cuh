@@ -46,6 +46,13 @@ __device__ __forceinline__ float mur(float u_in, float k, float un_in, float u_e
   return __fmaf_rn(k, __fsub_rn(un_in, u_edge), u_in);
 }
 
+// The same Mur update for the adjoint carried as w = (c dt)^2 l: with
+// r = coef_edge / coef_inner, coef_edge * (l_in + k (l_in' - l_edge)) equals
+// r w_in + k (r w_in' - w_edge).
+__device__ __forceinline__ float murw(float r, float w_in, float k, float wn_in, float w_edge) {
+  return mur(__fmul_rn(r, w_in), k, __fmul_rn(r, wn_in), w_edge);
+}
+
 __device__ __forceinline__ float corner_avg(float fx, float fy) {
   return __fmul_rn(0.5f, __fadd_rn(fx, fy));
 }

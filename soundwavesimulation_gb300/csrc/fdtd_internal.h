@@ -48,7 +48,7 @@ cudaError_t scatter_launch(int ny, int pitch, int n_shots, int n_nodes, const in
                            long long rx_stride, float* dense, cudaStream_t st);
 cudaError_t image_launch(int ny, int nx, int pitch, float idx2, float idy2, float cdiag,
                          int n_shots, const float* adj, const float* fwd, double scale,
-                         double* g, cudaStream_t st);
+                         const float* coef_div, double* g, cudaStream_t st);
 cudaError_t prepare_medium_launch(const double* c, int ny, int nx, int pitch, double dt,
                                   double dx, double dy, float* coef, float* mur,
                                   cudaStream_t st);

@@ -14,7 +14,7 @@ __device__ __forceinline__ float operand(const StepArgs& a, const float* u, int 
   if (y < 0 || y >= a.ny || x < 0 || x >= a.nx) return 0.f;
   const long long i = (long long)y * a.pitch + x;
   const float v = u[i];
-  return a.adjoint ? __fmul_rn(a.coef[i], v) : v;
+  return a.adjoint == 1 ? __fmul_rn(a.coef[i], v) : v;
 }
 
 // Interior update of node (y, x) of shot s, sources included, before Mur.
@@ -26,7 +26,8 @@ __device__ float cell_next(const StepArgs& a, int s, int y, int x) {
   const float nb = nbr4(operand(a, u, y, x - 1), operand(a, u, y, x + 1), operand(a, u, y - 1, x),
                         operand(a, u, y + 1, x), a.idx2, a.idy2);
   const float lap = __fmaf_rn(operand(a, u, y, x), a.cdiag, nb);
-  float un = a.adjoint ? leap_adj(u[i], uo[i], lap) : leap(u[i], uo[i], a.coef[i], lap);
+  // adjoint 1: l+ = 2l - l- + lap(coef l); adjoint 2 (w = coef l): the forward form
+  float un = a.adjoint == 1 ? leap_adj(u[i], uo[i], lap) : leap(u[i], uo[i], a.coef[i], lap);
   if (a.src_per_shot > 0) {
     float acc = 0.f;
     bool hit = false;
@@ -42,7 +43,10 @@ __device__ float cell_next(const StepArgs& a, int s, int y, int x) {
     }
     if (hit) un = inj_add(un, acc);
   }
-  if (a.dense) un = inj_add(un, a.dense[s * plane + i]);
+  if (a.dense) {
+    const float d = a.dense[s * plane + i];
+    un = inj_add(un, a.adjoint == 2 ? __fmul_rn(a.coef[i], d) : d);
+  }
   return un;
 }
 
@@ -61,23 +65,35 @@ __global__ void step_kernel(const StepArgs a) {
   const float* ckx = kt + nx;
   const float* cky = ckx + 4;
   const bool bot = y == 0, top = y == ny - 1, lef = x == 0, rig = x == nx - 1;
+  // ratios coef_edge / coef_inner for the w-form adjoint (1 otherwise)
+  const float* rw = a.mur + 2 * ny + 2 * nx + 8;
+  const bool wf = a.adjoint == 2;
+  auto R = [&](const float* arr, int j) { return wf ? arr[j] : 1.0f; };
+  const float* rl = rw;
+  const float* rr = rl + ny;
+  const float* rb = rr + ny;
+  const float* rt = rb + nx;
+  const float* crx = rt + nx;
+  const float* cry = crx + 4;
   float out;
   if (!(bot || top || lef || rig)) {
     out = cell_next(a, s, y, x);
   } else if (!(lef || rig)) {  // row 0 or ny-1 (fdtd2d/torch_backend.py:218-223)
     const int yi = bot ? 1 : ny - 2;
-    out = mur(u[yi * P + x], bot ? kb[x] : kt[x], cell_next(a, s, yi, x), u[y * P + x]);
+    out = murw(R(bot ? rb : rt, x), u[yi * P + x], bot ? kb[x] : kt[x], cell_next(a, s, yi, x),
+               u[y * P + x]);
   } else if (!(bot || top)) {  // column 0 or nx-1 (fdtd2d/torch_backend.py:212-217)
     const int xi = lef ? 1 : nx - 2;
-    out = mur(u[y * P + xi], lef ? kl[y] : kr[y], cell_next(a, s, y, xi), u[y * P + x]);
+    out = murw(R(lef ? rl : rr, y), u[y * P + xi], lef ? kl[y] : kr[y], cell_next(a, s, y, xi),
+               u[y * P + x]);
   } else {  // corner from the updated edges (fdtd2d/torch_backend.py:225-232)
     const int ci = (bot ? 0 : 2) + (lef ? 0 : 1);
     const int yi = bot ? 1 : ny - 2, xi = lef ? 1 : nx - 2;
     const float inner = cell_next(a, s, yi, xi);
-    const float ex = mur(u[yi * P + xi], bot ? kb[xi] : kt[xi], inner, u[y * P + xi]);
-    const float ey = mur(u[yi * P + xi], lef ? kl[yi] : kr[yi], inner, u[yi * P + x]);
-    const float fx = mur(u[y * P + xi], ckx[ci], ex, u[y * P + x]);
-    const float fy = mur(u[yi * P + x], cky[ci], ey, u[y * P + x]);
+    const float ex = murw(R(bot ? rb : rt, xi), u[yi * P + xi], bot ? kb[xi] : kt[xi], inner, u[y * P + xi]);
+    const float ey = murw(R(lef ? rl : rr, yi), u[yi * P + xi], lef ? kl[yi] : kr[yi], inner, u[yi * P + x]);
+    const float fx = murw(R(crx, ci), u[y * P + xi], ckx[ci], ex, u[y * P + x]);
+    const float fy = murw(R(cry, ci), u[yi * P + x], cky[ci], ey, u[y * P + x]);
     out = corner_avg(fx, fy);
   }
   a.u_next[s * plane + (long long)y * P + x] = out;
@@ -117,7 +133,7 @@ __device__ __forceinline__ float at0(const float* f, int ny, int nx, int pitch, 
 
 __global__ void image_kernel(int ny, int nx, int pitch, float idx2, float idy2, float cdiag,
                              int n_shots, const float* adj, const float* fwd, double scale,
-                             double* g) {
+                             const float* coef_div, double* g) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= nx || y >= ny) return;
@@ -130,7 +146,9 @@ __global__ void image_kernel(int ny, int nx, int pitch, float idx2, float idy2, 
                            at0(f, ny, nx, pitch, y + 1, x), idx2, idy2, cdiag);
     acc = __fmaf_rn(adj[s * plane + (long long)y * pitch + x], lap, acc);
   }
-  g[(long long)y * pitch + x] += (double)acc * scale;
+  // adjoint carried as w = coef * l: divide once by coef
+  const double a = coef_div ? (double)acc / (double)coef_div[(long long)y * pitch + x] : (double)acc;
+  g[(long long)y * pitch + x] += a * scale;
 }
 
 __device__ __forceinline__ double mur_k(double c, double dt, double h) {
@@ -149,31 +167,50 @@ __global__ void coef_kernel(const double* c, int ny, int nx, int pitch, double d
   coef[(long long)y * pitch + x] = v;
 }
 
+__device__ __forceinline__ float sq_ratio(double a, double b) { return (float)((a / b) * (a / b)); }
+
+// Mur coefficients, then (same layout, offset mur_len) the coefficient ratios
+// coef_edge / coef_inner = (c_edge / c_inner)^2 that the adjoint in w = coef * l
+// form needs.
 __global__ void mur_kernel(const double* c, int ny, int nx, double dt, double dx, double dy,
                            float* mur) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int len = 2 * ny + 2 * nx + 8;
   float* kl = mur;
   float* kr = kl + ny;
   float* kb = kr + ny;
   float* kt = kb + nx;
   float* ckx = kt + nx;
   float* cky = ckx + 4;
+  float* rl = mur + len;
+  float* rr = rl + ny;
+  float* rb = rr + ny;
+  float* rt = rb + nx;
+  float* crx = rt + nx;
+  float* cry = crx + 4;
+  auto C = [&](int y, int x) { return c[(long long)y * nx + x]; };
   if (i < ny) {
     const bool in = i >= 1 && i <= ny - 2;
-    kl[i] = in ? (float)mur_k(c[(long long)i * nx], dt, dx) : 0.f;
-    kr[i] = in ? (float)mur_k(c[(long long)i * nx + nx - 1], dt, dx) : 0.f;
+    kl[i] = in ? (float)mur_k(C(i, 0), dt, dx) : 0.f;
+    kr[i] = in ? (float)mur_k(C(i, nx - 1), dt, dx) : 0.f;
+    rl[i] = in ? sq_ratio(C(i, 0), C(i, 1)) : 0.f;
+    rr[i] = in ? sq_ratio(C(i, nx - 1), C(i, nx - 2)) : 0.f;
   }
   if (i < nx) {
     const bool in = i >= 1 && i <= nx - 2;
-    kb[i] = in ? (float)mur_k(c[i], dt, dy) : 0.f;
-    kt[i] = in ? (float)mur_k(c[(long long)(ny - 1) * nx + i], dt, dy) : 0.f;
+    kb[i] = in ? (float)mur_k(C(0, i), dt, dy) : 0.f;
+    kt[i] = in ? (float)mur_k(C(ny - 1, i), dt, dy) : 0.f;
+    rb[i] = in ? sq_ratio(C(0, i), C(1, i)) : 0.f;
+    rt[i] = in ? sq_ratio(C(ny - 1, i), C(ny - 2, i)) : 0.f;
   }
   if (i < 4) {
-    const int r = (i < 2) ? 0 : ny - 1;
-    const int col = (i & 1) ? nx - 1 : 0;
-    const double cc = c[(long long)r * nx + col];
+    const int r = (i < 2) ? 0 : ny - 1, ri = (i < 2) ? 1 : ny - 2;
+    const int col = (i & 1) ? nx - 1 : 0, ci = (i & 1) ? nx - 2 : 1;
+    const double cc = C(r, col);
     ckx[i] = (float)mur_k(cc, dt, dx);
     cky[i] = (float)mur_k(cc, dt, dy);
+    crx[i] = sq_ratio(cc, C(r, ci));
+    cry[i] = sq_ratio(cc, C(ri, col));
   }
 }
 
@@ -289,11 +326,11 @@ cudaError_t scatter_launch(int ny, int pitch, int n_shots, int n_nodes, const in
 
 cudaError_t image_launch(int ny, int nx, int pitch, float idx2, float idy2, float cdiag,
                          int n_shots, const float* adj, const float* fwd, double scale,
-                         double* g, cudaStream_t st) {
+                         const float* coef_div, double* g, cudaStream_t st) {
   dim3 block(32, 8);
   dim3 grid((nx + 31) / 32, (ny + 7) / 8);
   image_kernel<<<grid, block, 0, st>>>(ny, nx, pitch, idx2, idy2, cdiag, n_shots, adj, fwd,
-                                       scale, g);
+                                       scale, coef_div, g);
   return cudaGetLastError();
 }
 

@@ -447,7 +447,8 @@ int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, co
   a.wave_len = waveform_len;
   a.step = step;
   a.dense = dense;
-  a.adjoint = adjoint ? 1 : 0;
+  if (adjoint < 0 || adjoint > 2) return fail(FDTD_ERR_INVALID, "adjoint must be 0, 1 or 2");
+  a.adjoint = adjoint;
   cudaError_t e = step_launch(a, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "step");
   return FDTD_OK;
@@ -482,7 +483,7 @@ int32_t fdtd_image(const fdtd_grid* grid, int32_t n_shots, const float* adj, con
   if (!grid || !adj || !fwd || !g) return fail(FDTD_ERR_INVALID, "null pointer");
   const double idx2 = 1.0 / (grid->dx * grid->dx), idy2 = 1.0 / (grid->dy * grid->dy);
   cudaError_t e = image_launch(grid->ny, grid->nx, grid->pitch, (float)idx2, (float)idy2,
-                               (float)(-2.0 * (idx2 + idy2)), n_shots, adj, fwd, scale, g,
+                               (float)(-2.0 * (idx2 + idy2)), n_shots, adj, fwd, scale, nullptr, g,
                                (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "image");
   return FDTD_OK;
@@ -958,12 +959,14 @@ int32_t fdtd_gradient_plain(const fdtd_problem* prob, const float* observed, con
     for (int n = nt - 1; n >= 0; --n) {
       e = scatter_launch(g.ny, g.pitch, 1, n_nodes, tap_nodes, tap_w, resid + n, 0, nt, dense, st);
       if (e != cudaSuccess) return cuda_fail(e, "plain scatter");
+      // the adjoint in w = coef * l form, as the fused engine carries it
       rc = fdtd_step(&g, 1, lam + (size_t)io * plane, lam + (size_t)ic * plane, lam + (size_t)in * plane, 0,
-                     nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, dense, 1, stream);
+                     nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, dense, 2, stream);
       if (rc) return rc;
       if (n >= 1) {
         e = image_launch(g.ny, g.nx, g.pitch, (float)idx2, (float)idy2, (float)(-2.0 * (idx2 + idy2)), 1,
-                         lam + (size_t)in * plane, hist + (size_t)(n + 1) * plane, g.dt * g.dt, grad_c2, st);
+                         lam + (size_t)in * plane, hist + (size_t)(n + 1) * plane, g.dt * g.dt, g.coef,
+                         grad_c2, st);
         if (e != cudaSuccess) return cuda_fail(e, "plain image");
       }
       const int t = io; io = ic; ic = in; in = t;

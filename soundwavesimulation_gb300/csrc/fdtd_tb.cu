@@ -49,12 +49,9 @@ struct Ctx {
   const int* s_srcpos;
 };
 
-template <int MODE>
-__device__ __forceinline__ float4 opval(const float (&v)[4], float4 co) {
-  if (MODE == MODE_ADJ) {
-    return make_float4(__fmul_rn(co.x, v[0]), __fmul_rn(co.y, v[1]), __fmul_rn(co.z, v[2]),
-                       __fmul_rn(co.w, v[3]));
-  }
+// Stencil operand of one band row: the field itself in every mode (the adjoint
+// is carried as w = (c dt)^2 l, so its update has the forward's form).
+__device__ __forceinline__ float4 opval(const float (&v)[4]) {
   return make_float4(v[0], v[1], v[2], v[3]);
 }
 
@@ -117,7 +114,7 @@ __device__ __forceinline__ void prefetch_lap(const TbParams& p, const Ctx& x, in
 // the recompute stores is exact; in the adjoint their operand coef * l is zero,
 // so whatever they hold never reaches a domain cell, and they are never written
 // back.
-template <int KY>
+template <int KY, bool WF>
 __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY][4],
                                          const TbParams& p, const Ctx& x) {
   const int nx = p.nx, ny = p.ny;
@@ -127,6 +124,14 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
   const float* kt = kb + nx;
   const float* ckx = kt + nx;
   const float* cky = ckx + 4;
+  // w-form adjoint: the inner values scale by coef_edge / coef_inner (1 otherwise)
+  const float* rlw = p.mur + 2 * ny + 2 * nx + 8;
+  const float* rrw = rlw + ny;
+  const float* rbw = rrw + ny;
+  const float* rtw = rbw + nx;
+  const float* crx = rtw + nx;
+  const float* cry = crx + 4;
+  auto R = [&](const float* arr, int j) { return WF ? __ldg(arr + j) : 1.0f; };
   const int rb = -x.y0;          // band row of global row 0
   const int rt = ny - 1 - x.y0;  // band row of global row ny-1
   const bool has_bot = (x.flags & TF_BOTTOM) && rb >= 0 && rb + 1 < KY;   // warp-uniform
@@ -138,7 +143,7 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           const int xx = x.xb + c;
-          if (xx >= 1 && xx <= nx - 2) P[r][c] = mur(C[r + 1][c], __ldg(kb + xx), P[r + 1][c], C[r][c]);
+          if (xx >= 1 && xx <= nx - 2) P[r][c] = murw(R(rbw, xx), C[r + 1][c], __ldg(kb + xx), P[r + 1][c], C[r][c]);
         }
       }
     }
@@ -150,7 +155,7 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           const int xx = x.xb + c;
-          if (xx >= 1 && xx <= nx - 2) P[r][c] = mur(C[r - 1][c], __ldg(kt + xx), P[r - 1][c], C[r][c]);
+          if (xx >= 1 && xx <= nx - 2) P[r][c] = murw(R(rtw, xx), C[r - 1][c], __ldg(kt + xx), P[r - 1][c], C[r][c]);
         }
       }
     }
@@ -159,7 +164,7 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
       const int yy = x.y0 + r;
-      if (yy >= 1 && yy <= ny - 2) P[r][0] = mur(C[r][1], __ldg(kl + yy), P[r][1], C[r][0]);
+      if (yy >= 1 && yy <= ny - 2) P[r][0] = murw(R(rlw, yy), C[r][1], __ldg(kl + yy), P[r][1], C[r][0]);
     }
   }
   if (x.flags & TF_RIGHT) {
@@ -182,7 +187,7 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
           if (c == c1) {
             const float uin = (c == 0) ? su : C[r][c > 0 ? c - 1 : 0];
             const float nin = (c == 0) ? sn : P[r][c > 0 ? c - 1 : 0];
-            P[r][c] = mur(uin, __ldg(kr + yy), nin, C[r][c]);
+            P[r][c] = murw(R(rrw, yy), uin, __ldg(kr + yy), nin, C[r][c]);
           }
         }
       }
@@ -206,8 +211,8 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
               if (c == c1) {
                 const float uin = (c == 0) ? su : C[r][c > 0 ? c - 1 : 0];
                 const float nin = (c == 0) ? sn : P[r][c > 0 ? c - 1 : 0];
-                const float fx = mur(uin, __ldg(ckx + ci), nin, C[r][c]);
-                const float fy = mur(C[rn][c], __ldg(cky + ci), P[rn][c], C[r][c]);
+                const float fx = murw(R(crx, ci), uin, __ldg(ckx + ci), nin, C[r][c]);
+                const float fy = murw(R(cry, ci), C[rn][c], __ldg(cky + ci), P[rn][c], C[r][c]);
                 P[r][c] = corner_avg(fx, fy);
               }
             }
@@ -224,8 +229,8 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
       if (bot || top) {
         const int rn = bot ? (r + 1 < KY ? r + 1 : r) : (r >= 1 ? r - 1 : r);
         const int ci = bot ? 0 : 2;
-        const float fx = mur(C[r][1], __ldg(ckx + ci), P[r][1], C[r][0]);
-        const float fy = mur(C[rn][0], __ldg(cky + ci), P[rn][0], C[r][0]);
+        const float fx = murw(R(crx, ci), C[r][1], __ldg(ckx + ci), P[r][1], C[r][0]);
+        const float fy = murw(R(cry, ci), C[rn][0], __ldg(cky + ci), P[rn][0], C[r][0]);
         P[r][0] = corner_avg(fx, fy);
       }
     }
@@ -245,7 +250,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   // ---- stencil over the band, rolling the row above / below
   float4 prv = (x.w > 0) ? xin[(x.w - 1) * 64 + 32 + x.lane] : zero4;
   const float4 below = (x.w < x.nw - 1) ? xin[(x.w + 1) * 64 + x.lane] : zero4;
-  float4 cur = opval<MODE>(C[0], coefrow<MODE>(p, x, coef4, 0));
+  float4 cur = opval(C[0]);
   const bool lzero = EDGE && x.lane == 0 && x.rx0 == 0;
   const bool rzero = EDGE && x.lane == 31 && (x.rx0 + RX >= p.nx);
   float* segrow = nullptr;
@@ -255,7 +260,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
 #pragma unroll
   for (int r = 0; r < KY; ++r) {
-    const float4 nxt = (r + 1 < KY) ? opval<MODE>(C[r + 1], coefrow<MODE>(p, x, coef4, r + 1)) : below;
+    const float4 nxt = (r + 1 < KY) ? opval(C[r + 1]) : below;
     float lft = __shfl_up_sync(FULL, cur.w, 1);
     float rgt = __shfl_down_sync(FULL, cur.x, 1);
     if (lzero) lft = 0.f;
@@ -264,13 +269,8 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
     const float n1 = nbr4(cur.x, cur.z, prv.y, nxt.y, idx2, idy2);
     const float n2 = nbr4(cur.y, cur.w, prv.z, nxt.z, idx2, idy2);
     const float n3 = nbr4(cur.z, rgt, prv.w, nxt.w, idx2, idy2);
-    if (MODE == MODE_ADJ) {
-      P[r][0] = leap_adj(C[r][0], P[r][0], __fmaf_rn(cur.x, cdiag, n0));
-      P[r][1] = leap_adj(C[r][1], P[r][1], __fmaf_rn(cur.y, cdiag, n1));
-      P[r][2] = leap_adj(C[r][2], P[r][2], __fmaf_rn(cur.z, cdiag, n2));
-      P[r][3] = leap_adj(C[r][3], P[r][3], __fmaf_rn(cur.w, cdiag, n3));
-    } else {
-      const float4 co = coef4[r * 32];
+    {
+      const float4 co = coefrow<MODE>(p, x, coef4, r);
       const float l0 = __fmaf_rn(cur.x, cdiag, n0), l1 = __fmaf_rn(cur.y, cdiag, n1);
       const float l2 = __fmaf_rn(cur.z, cdiag, n2), l3 = __fmaf_rn(cur.w, cdiag, n3);
       if (MODE == MODE_REC && ((x.own_rows >> r) & 1u)) {
@@ -319,7 +319,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
 
   // ---- Mur edges and corners, zero outside the domain
-  if (EDGE) boundary<KY>(P, C, p, x);
+  if (EDGE) boundary<KY, MODE == MODE_ADJ>(P, C, p, x);
 
   // ---- receiver taps (forward) / imaging (adjoint)
   if (MODE == MODE_FWD && x.mask) {
@@ -357,8 +357,8 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
 
   // ---- publish the band's first and last rows for the next step
-  xout[x.w * 64 + x.lane] = opval<MODE>(P[0], coefrow<MODE>(p, x, coef4, 0));
-  xout[x.w * 64 + 32 + x.lane] = opval<MODE>(P[KY - 1], coefrow<MODE>(p, x, coef4, KY - 1));
+  xout[x.w * 64 + x.lane] = opval(P[0]);
+  xout[x.w * 64 + 32 + x.lane] = opval(P[KY - 1]);
   __syncthreads();
 }
 
@@ -411,8 +411,8 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
     }
   }
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
-  x.s_xch[x.w * 64 + x.lane] = opval<MODE>(C[0], coefrow<MODE>(p, x, coef4, 0));
-  x.s_xch[x.w * 64 + 32 + x.lane] = opval<MODE>(C[KY - 1], coefrow<MODE>(p, x, coef4, KY - 1));
+  x.s_xch[x.w * 64 + x.lane] = opval(C[0]);
+  x.s_xch[x.w * 64 + 32 + x.lane] = opval(C[KY - 1]);
   if (MODE == MODE_ADJ && x.own_rows && x.own_cols && p.n0 >= 1) prefetch_lap<KY>(p, x, p.n0);
   __syncthreads();
 
@@ -453,6 +453,9 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   const int RY = nw * KY;
   const int nitems = p.ntiles * p.nshots;
 
+  // Items are (tile, shot) pairs with shots varying fastest, dealt out with a
+  // grid stride: at any moment the CTAs hold a mix of edge, interior and
+  // receiver-heavy tiles, which balances better than contiguous runs per CTA.
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     const int ti = item / p.nshots;
     const int s = item - ti * p.nshots;
@@ -545,7 +548,10 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
           const int rl = tp.rloc[q];
           if (rl >= 0) acc = inj_acc(acc, tp.w[q], s_res[rl * p.tmax + k]);
         }
-        x.s_tap[k * p.ntap_max + ti2] = acc;
+        // the adjoint is carried as w = coef * l: scale the injection by the node's coef
+        const int pt = tp.packed >> 8, pb = tp.packed & 255;
+        const int gy = t.ry0 + (pt >> 5) * KY + (pb >> 2), gx = t.rx0 + (pt & 31) * 4 + (pb & 3);
+        x.s_tap[k * p.ntap_max + ti2] = __fmul_rn(__ldg(p.coef + (long long)gy * p.pitch + gx), acc);
       }
     }
     x.mask = s_mask[x.tid];
@@ -582,12 +588,17 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
 #pragma unroll
       for (int r = 0; r < KY; ++r) {
         if ((x.own_rows >> r) & 1u) {
+          // the tile summed w * lap with w = coef * l: divide by coef once here, in
+          // float32 (GB300's float64 pipe is ~64x slower); only the cross-item sum
+          // (the atomic) is float64
           const float4 gv = g4[r * 32];
+          const float4 co = ldg4(x.gcoef + (long long)r * p.pitch);
+          const float sc = (float)p.scale;
           double* gd = p.grad + (long long)(x.y0 + r) * p.pitch + x.xb;
-          if (x.own_cols & 1u) atomicAdd(gd + 0, (double)gv.x * p.scale);
-          if (x.own_cols & 2u) atomicAdd(gd + 1, (double)gv.y * p.scale);
-          if (x.own_cols & 4u) atomicAdd(gd + 2, (double)gv.z * p.scale);
-          if (x.own_cols & 8u) atomicAdd(gd + 3, (double)gv.w * p.scale);
+          if (x.own_cols & 1u) atomicAdd(gd + 0, (double)(__fdiv_rn(gv.x, co.x) * sc));
+          if (x.own_cols & 2u) atomicAdd(gd + 1, (double)(__fdiv_rn(gv.y, co.y) * sc));
+          if (x.own_cols & 4u) atomicAdd(gd + 2, (double)(__fdiv_rn(gv.z, co.z) * sc));
+          if (x.own_cols & 8u) atomicAdd(gd + 3, (double)(__fdiv_rn(gv.w, co.w) * sc));
         }
       }
     }

@@ -57,7 +57,7 @@ class DeviceMedium:
         self.dx, self.dy, self.dt = float(dx), float(dy), float(dt)
         self.c64 = c64
         self.coef = torch.zeros((self.ny, self.pitch), dtype=torch.float32, device=self.device)
-        self.mur = torch.zeros(2 * self.ny + 2 * self.nx + 8, dtype=torch.float32, device=self.device)
+        self.mur = torch.zeros(2 * (2 * self.ny + 2 * self.nx + 8), dtype=torch.float32, device=self.device)
         self.prepare()
 
     def set_c(self, c):
