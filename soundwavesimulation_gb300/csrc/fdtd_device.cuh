@@ -91,18 +91,20 @@ struct TbTile {
   int tap_off, ntap;     // receiver tap nodes inside the region
   int rxl_off, nrxl;     // receivers with a tap inside the region
   int rec_off, nrec;     // receivers whose samples this tile records
-  int pad0, pad1, pad2;
+  int nrow;              // staged tap rows: (thread, band row) pairs holding a tap node
+  int pad1, pad2;
 };
 
 struct TbTap {           // one receiver tap node inside a tile
   int packed;            // (thread << 8) | (row_in_lane * 4 + column_in_lane)
+  int srow;              // staged tap row holding this node (its float is srow * 4 + column)
   int rloc[TAP_C];       // tile-local receiver index of each contribution, -1 = none
   float w[TAP_C];
 };
 
 struct TbRec {           // one receiver recorded by a tile
   int rg;                // global receiver index
-  int slot[4];           // tile-local tap slots of (r0,c0), (r0,c1), (r1,c0), (r1,c1)
+  int slot[4];           // staged floats (srow * 4 + column) of (r0,c0), (r0,c1), (r1,c0), (r1,c1)
   float w[4];
 };
 
@@ -124,7 +126,7 @@ struct TbParams {
   const TbTap* taps;
   const int* rxl;
   const TbRec* recs;
-  int ntap_max, nrxl_max, tmax;
+  int nrow_max, nrxl_max, tmax;  // nrow_max: staged tap rows of the largest tile
   // sources
   const SrcNode* src;    // (nshots, SRC_MAX)
   const int* nsrc;       // (nshots)
@@ -157,7 +159,7 @@ struct TbSmem {
 
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
 
-__host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int ntap_max,
+__host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int nrow_max,
                                                  int nrxl_max, int tmax) {
   TbSmem m;
   const size_t region = size_t(nw) * ky * RX * sizeof(float);
@@ -170,7 +172,10 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
   off += region;
   m.g = off; if (mode == MODE_ADJ) off += region;
   m.xch = off; off += size_t(2) * nw * 2 * 32 * 16;
-  m.tap = off; off += tb_align16(size_t(tmax) * (ntap_max > 0 ? ntap_max : 1) * sizeof(float));
+  // tap stage: per step, the full 4-cell row of every (thread, band row) that holds
+  // a receiver tap node (forward: recorded values; adjoint: injections, zero
+  // where a row's cell has no tap)
+  m.tap = off; off += size_t(tmax) * (nrow_max > 0 ? nrow_max : 1) * 4 * sizeof(float);
   m.res = off; if (mode == MODE_ADJ) off += tb_align16(size_t(nrxl_max > 0 ? nrxl_max : 1) * tmax * sizeof(float));
   m.src = off; off += tb_align16(size_t(tmax) * SRC_MAX * sizeof(float));
   m.mask = off; off += size_t(nw) * 32 * sizeof(unsigned);

@@ -105,7 +105,7 @@ struct fdtd_plan {
   std::vector<TbRec> recs;
   std::vector<SrcNode> src;
   std::vector<int> nsrc;
-  int ntap_max = 0, nrxl_max = 0;
+  int nrow_max = 0, nrxl_max = 0;
   int ckpt_every = 0, nseg = 1;
   size_t field_elems = 0;
   // workspace offsets
@@ -152,7 +152,7 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.taps = reinterpret_cast<const TbTap*>(p->ws + p->o_taps);
   q.rxl = reinterpret_cast<const int*>(p->ws + p->o_rxl);
   q.recs = reinterpret_cast<const TbRec*>(p->ws + p->o_recs);
-  q.ntap_max = p->ntap_max;
+  q.nrow_max = p->nrow_max;
   q.nrxl_max = p->nrxl_max;
   q.tmax = p->tmax;
   q.src = reinterpret_cast<const SrcNode*>(p->ws + p->o_src);
@@ -224,7 +224,7 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
   p->taps.clear();
   p->rxl.clear();
   p->recs.clear();
-  p->ntap_max = 0;
+  p->nrow_max = 0;
   p->nrxl_max = 0;
   std::vector<int> recorded(R, 0);
   for (const AxisTile& ay : ty) {
@@ -258,10 +258,14 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
       for (auto& kv : rloc) { kv.second = (int)rx_here.size(); rx_here.push_back(kv.first); }
       t.tap_off = (int)p->taps.size();
       t.ntap = (int)local.size();
-      std::map<int, int> slot_of_node;
+      std::map<int, int> slot_of_node;  // node id -> staged float (srow * 4 + column)
+      t.nrow = 0;
       for (size_t i = 0; i < local.size(); ++i) {
         TbTap tp;
         tp.packed = local[i].first;
+        // taps are sorted by (thread, row, column): a new (thread, row) pair opens a staged row
+        if (i == 0 || (local[i].first >> 2) != (local[i - 1].first >> 2)) ++t.nrow;
+        tp.srow = t.nrow - 1;
         for (int q = 0; q < TAP_C; ++q) { tp.rloc[q] = -1; tp.w[q] = 0.f; }
         const auto& cl = contrib[local[i].second];
         for (size_t q = 0; q < cl.size(); ++q) {
@@ -269,7 +273,7 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
           tp.w[q] = cl[q].second;
         }
         p->taps.push_back(tp);
-        slot_of_node[local[i].second] = (int)i;
+        slot_of_node[local[i].second] = tp.srow * 4 + (tp.packed & 3);
       }
       t.rxl_off = (int)p->rxl.size();
       t.nrxl = (int)rx_here.size();
@@ -291,7 +295,7 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
         recorded[r]++;
       }
       t.nrec = (int)p->recs.size() - t.rec_off;
-      p->ntap_max = std::max(p->ntap_max, t.ntap);
+      p->nrow_max = std::max(p->nrow_max, t.nrow);
       p->nrxl_max = std::max(p->nrxl_max, t.nrxl);
       p->tiles.push_back(t);
     }
@@ -572,7 +576,7 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   rc = build_tables(p, problem);
   if (rc) { delete p; return rc; }
   for (int m = 0; m < 3; ++m) {
-    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->ntap_max, p->nrxl_max, p->tmax).total;
+    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->nrow_max, p->nrxl_max, p->tmax).total;
     if (p->smem[m] > SMEM_LIMIT && (m == MODE_FWD || for_gradient)) {
       delete p;
       return fail(FDTD_ERR_UNSUPPORTED, "shared memory need exceeds 227 KB; use fewer steps per launch or warps");

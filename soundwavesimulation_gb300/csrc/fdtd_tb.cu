@@ -307,12 +307,17 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
       }
     }
   } else if (x.mask) {
-    int slot = x.base;
-    const float* inj = x.s_tap + k * p.ntap_max;
+    // residual injection: whole staged rows, zero where a cell holds no tap
+    const float4* inj = reinterpret_cast<const float4*>(x.s_tap) + k * p.nrow_max + x.base;
+    int slot = 0;
 #pragma unroll
-    for (int b = 0; b < 4 * KY; ++b) {
-      if ((x.mask >> b) & 1u) {
-        P[b >> 2][b & 3] = inj_add(P[b >> 2][b & 3], inj[slot]);
+    for (int r = 0; r < KY; ++r) {
+      if ((x.mask >> r) & 1u) {
+        const float4 v = inj[slot];
+        P[r][0] = inj_add(P[r][0], v.x);
+        P[r][1] = inj_add(P[r][1], v.y);
+        P[r][2] = inj_add(P[r][2], v.z);
+        P[r][3] = inj_add(P[r][3], v.w);
         ++slot;
       }
     }
@@ -323,12 +328,13 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
 
   // ---- receiver taps (forward) / imaging (adjoint)
   if (MODE == MODE_FWD && x.mask) {
-    int slot = x.base;
-    float* rec = x.s_tap + k * p.ntap_max;
+    // stage every band row that holds a tap node, all four cells of it
+    float4* rec = reinterpret_cast<float4*>(x.s_tap) + k * p.nrow_max + x.base;
+    int slot = 0;
 #pragma unroll
-    for (int b = 0; b < 4 * KY; ++b) {
-      if ((x.mask >> b) & 1u) {
-        rec[slot] = P[b >> 2][b & 3];
+    for (int r = 0; r < KY; ++r) {
+      if ((x.mask >> r) & 1u) {
+        rec[slot] = make_float4(P[r][0], P[r][1], P[r][2], P[r][3]);
         ++slot;
       }
     }
@@ -432,7 +438,7 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = p.nwarps;
   const int nthr = nw * 32;
-  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.ntap_max, p.nrxl_max, p.tmax);
+  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax);
   Ctx x;
   x.tid = threadIdx.x;
   x.w = x.tid >> 5;
@@ -525,6 +531,11 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
         s_src[i] = acc;
       }
     } else {
+      // staged injection rows start at zero: cells without a tap add nothing
+      for (int i = x.tid; i < p.nsteps * t.nrow; i += nthr) {
+        const int k = i / t.nrow, j = i - k * t.nrow;
+        reinterpret_cast<float4*>(x.s_tap)[k * p.nrow_max + j] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
       for (int i = x.tid; i < t.nrxl * p.nsteps; i += nthr) {
         const int j = i / p.nsteps, k = i - j * p.nsteps;
         const int rg = __ldg(p.rxl + t.rxl_off + j);
@@ -532,10 +543,11 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
       }
     }
     __syncthreads();
+    // per thread: which band rows hold tap nodes, and the first staged row
     for (int i = x.tid; i < t.ntap; i += nthr) {
-      const int pk = p.taps[t.tap_off + i].packed;
-      atomicOr(&s_mask[pk >> 8], 1u << (pk & 255));
-      atomicMin(&s_base[pk >> 8], i);
+      const TbTap& tp = p.taps[t.tap_off + i];
+      atomicOr(&s_mask[tp.packed >> 8], 1u << ((tp.packed & 255) >> 2));
+      atomicMin(&s_base[tp.packed >> 8], tp.srow);
     }
     __syncthreads();
     if (MODE == MODE_ADJ) {
@@ -551,7 +563,8 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
         // the adjoint is carried as w = coef * l: scale the injection by the node's coef
         const int pt = tp.packed >> 8, pb = tp.packed & 255;
         const int gy = t.ry0 + (pt >> 5) * KY + (pb >> 2), gx = t.rx0 + (pt & 31) * 4 + (pb & 3);
-        x.s_tap[k * p.ntap_max + ti2] = __fmul_rn(__ldg(p.coef + (long long)gy * p.pitch + gx), acc);
+        x.s_tap[(k * p.nrow_max + tp.srow) * 4 + (pb & 3)] =
+            __fmul_rn(__ldg(p.coef + (long long)gy * p.pitch + gx), acc);
       }
     }
     x.mask = s_mask[x.tid];
@@ -577,7 +590,7 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
       for (int i = x.tid; i < t.nrec * p.nsteps; i += nthr) {
         const int j = i / p.nsteps, k = i - j * p.nsteps;
         const TbRec& rc = p.recs[t.rec_off + j];
-        const float* v = x.s_tap + k * p.ntap_max;
+        const float* v = x.s_tap + (long long)k * p.nrow_max * 4;
         const float smp = gather4(v[rc.slot[0]], v[rc.slot[1]], v[rc.slot[2]], v[rc.slot[3]],
                                   rc.w[0], rc.w[1], rc.w[2], rc.w[3]);
         p.traces[((long long)s * p.nrx + rc.rg) * p.nt + p.n0 + k] = smp;
