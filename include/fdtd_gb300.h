@@ -95,7 +95,7 @@ typedef struct fdtd_problem {
 /* Launch shape of the temporally blocked engine. Zero fields take defaults. */
 typedef struct fdtd_tuning {
   int32_t rows_per_lane;    /* rows each lane keeps in registers: 4 or 8 */
-  int32_t warps;            /* warps per CTA (region height = warps * rows_per_lane) */
+  int32_t warps;            /* warps per CTA, 2..16 (2..32 with 4 rows per lane); region height = warps * rows_per_lane */
   int32_t steps_per_launch; /* leapfrog steps per HBM round trip (temporal block) */
   int32_t ckpt_every;       /* checkpoint spacing in steps, rounded up to a multiple of
                                steps_per_launch; 0 = about sqrt(2 nt) */

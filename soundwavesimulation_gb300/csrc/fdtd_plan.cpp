@@ -535,7 +535,7 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   if (tuning) t = *tuning;
   if (t.rows_per_lane == 0) t.rows_per_lane = 8;
   if (t.rows_per_lane != 4 && t.rows_per_lane != 8) { delete p; return fail(FDTD_ERR_UNSUPPORTED, "rows_per_lane must be 4 or 8"); }
-  const int max_warps = 16;
+  const int max_warps = t.rows_per_lane == 4 ? 32 : 16;
   if (t.warps == 0) t.warps = 16;
   if (t.warps < 2 || t.warps > max_warps) { delete p; return fail(FDTD_ERR_UNSUPPORTED, "warps out of range"); }
   if (t.steps_per_launch == 0) {

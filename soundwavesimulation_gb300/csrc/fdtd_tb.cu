@@ -245,7 +245,11 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   const float4* xin = x.s_xch + (k & 1) * x.nw * 64;
   float4* xout = x.s_xch + ((k + 1) & 1) * x.nw * 64;
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
-  const float idx2 = p.idx2, idy2 = p.idy2, cdiag = p.cdiag;
+  // Paired-lane (f32x2) arithmetic: every element is rounded once, exactly like the
+  // scalar helpers of fdtd_device.cuh, so the values stay bit-identical to the
+  // one-step kernels while one instruction updates two cells.
+  const float2 I2 = make_float2(p.idx2, p.idx2), J2 = make_float2(p.idy2, p.idy2);
+  const float2 D2 = make_float2(p.cdiag, p.cdiag), TWO2 = make_float2(2.0f, 2.0f);
 
   // ---- stencil over the band, rolling the row above / below
   float4 prv = (x.w > 0) ? xin[(x.w - 1) * 64 + 32 + x.lane] : zero4;
@@ -265,14 +269,18 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
     float rgt = __shfl_down_sync(FULL, cur.x, 1);
     if (lzero) lft = 0.f;
     if (rzero) rgt = 0.f;
-    const float n0 = nbr4(lft, cur.y, prv.x, nxt.x, idx2, idy2);
-    const float n1 = nbr4(cur.x, cur.z, prv.y, nxt.y, idx2, idy2);
-    const float n2 = nbr4(cur.y, cur.w, prv.z, nxt.z, idx2, idy2);
-    const float n3 = nbr4(cur.z, rgt, prv.w, nxt.w, idx2, idy2);
+    // nbr4 / lap5 / leap of fdtd_device.cuh on cell pairs (0,1) and (2,3)
+    const float2 udA = __fadd2_rn(make_float2(prv.x, prv.y), make_float2(nxt.x, nxt.y));
+    const float2 udB = __fadd2_rn(make_float2(prv.z, prv.w), make_float2(nxt.z, nxt.w));
+    const float2 lrA = __fadd2_rn(make_float2(lft, cur.x), make_float2(cur.y, cur.z));
+    const float2 lrB = __fadd2_rn(make_float2(cur.y, cur.z), make_float2(cur.w, rgt));
+    const float2 nA = __ffma2_rn(udA, J2, __fmul2_rn(lrA, I2));
+    const float2 nB = __ffma2_rn(udB, J2, __fmul2_rn(lrB, I2));
     {
       const float4 co = coefrow<MODE>(p, x, coef4, r);
-      const float l0 = __fmaf_rn(cur.x, cdiag, n0), l1 = __fmaf_rn(cur.y, cdiag, n1);
-      const float l2 = __fmaf_rn(cur.z, cdiag, n2), l3 = __fmaf_rn(cur.w, cdiag, n3);
+      const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), D2, nA);
+      const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), D2, nB);
+      const float l0 = lA.x, l1 = lA.y, l2 = lB.x, l3 = lB.y;
       if (MODE == MODE_REC && ((x.own_rows >> r) & 1u)) {
         float* dst = segrow + (long long)r * p.pitch;
         if (x.own_cols == 0xFu) {
@@ -284,10 +292,14 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
           if (x.own_cols & 8u) dst[3] = l3;
         }
       }
-      P[r][0] = leap(C[r][0], P[r][0], co.x, l0);
-      P[r][1] = leap(C[r][1], P[r][1], co.y, l1);
-      P[r][2] = leap(C[r][2], P[r][2], co.z, l2);
-      P[r][3] = leap(C[r][3], P[r][3], co.w, l3);
+      const float2 tA = __ffma2_rn(TWO2, make_float2(cur.x, cur.y), make_float2(-P[r][0], -P[r][1]));
+      const float2 tB = __ffma2_rn(TWO2, make_float2(cur.z, cur.w), make_float2(-P[r][2], -P[r][3]));
+      const float2 uA = __ffma2_rn(make_float2(co.x, co.y), lA, tA);
+      const float2 uB = __ffma2_rn(make_float2(co.z, co.w), lB, tB);
+      P[r][0] = uA.x;
+      P[r][1] = uA.y;
+      P[r][2] = uB.x;
+      P[r][3] = uB.y;
     }
     prv = cur;
     cur = nxt;
@@ -642,13 +654,15 @@ cudaError_t launch_mode(const TbParams& p, int mode, int grid, size_t smem, cuda
 }  // namespace
 
 // Instantiations: KY = 8 rows per lane with at most 12 warps (168 registers per
-// thread, no spills) or 16 warps (128 registers); KY = 4 with at most 16 warps.
+// thread, no spills) or 16 warps (128 registers); KY = 4 with at most 16 warps
+// (128 registers) or 32 warps (64 registers).
 cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st) {
   if (ky == 8) {
     if (p.nwarps <= 12) return launch_mode<8, 384>(p, mode, grid, smem, st);
     return launch_mode<8, 512>(p, mode, grid, smem, st);
   }
-  return launch_mode<4, 512>(p, mode, grid, smem, st);
+  if (p.nwarps <= 16) return launch_mode<4, 512>(p, mode, grid, smem, st);
+  return launch_mode<4, 1024>(p, mode, grid, smem, st);
 }
 
 }  // namespace fdtd

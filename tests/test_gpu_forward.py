@@ -180,6 +180,7 @@ def _oracle_forward(p, nt):
     (129, 128, 2, 25, {"steps_per_launch": 1}),
     (200, 140, 2, 37, {"steps_per_launch": 3, "rows_per_lane": 4, "warps": 10}),
     (300, 211, 2, 47, {"steps_per_launch": 11, "rows_per_lane": 8, "warps": 12}),
+    (260, 300, 2, 41, {"steps_per_launch": 9, "rows_per_lane": 4, "warps": 32}),
 ])
 def test_fused_engine_shapes_and_tunings(tb, ny, nx, shots, nt, tuning):
     """Odd sizes, several tiles, edge-straddling receivers, multi-node sources, every tuning family."""

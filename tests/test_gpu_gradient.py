@@ -107,8 +107,11 @@ def test_checkpoint_spacing_and_16bit_storage(mods, golden):
         assert rel(g, g_ref) < (1e-3 if wd == torch.float16 else 5e-3)
 
 
-def test_fused_gradient_equals_plain_form(mods):
-    """Checkpointed fused gradient vs the plain per-shot full-history gradient."""
+@pytest.mark.parametrize("tuning", [{"steps_per_launch": 10},
+                                    {"steps_per_launch": 9, "rows_per_lane": 4, "warps": 32},
+                                    {"steps_per_launch": 7, "rows_per_lane": 8, "warps": 12}])
+def test_fused_gradient_equals_plain_form(mods, tuning):
+    """Checkpointed fused gradient vs the plain per-shot full-history gradient, per launch shape."""
     from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan, ProblemTables, gradient_plain
     from soundwavesimulation_gb300.engine import residual_misfit
     from soundwavesimulation_gb300.phantoms import random_ellipses
@@ -125,8 +128,7 @@ def test_fused_gradient_equals_plain_form(mods):
     true = DeviceMedium(c, dx, dx, dt, "cuda")
     observed = FusedPlan(true, ring.receiver_taps(), src, waves, nt).forward().clone()
     start = DeviceMedium(np.where(c > 1500.0, 0.5 * (c + 1500.0), c), dx, dx, dt, "cuda")
-    plan = FusedPlan(start, ring.receiver_taps(), src, waves, nt, for_gradient=True,
-                     tuning={"steps_per_launch": 10})
+    plan = FusedPlan(start, ring.receiver_taps(), src, waves, nt, for_gradient=True, tuning=tuning)
     traces = plan.forward(save_checkpoints=True)
     res, J = residual_misfit(traces, observed, tx)
     g = torch.zeros((n, start.pitch), dtype=torch.float64, device="cuda")
