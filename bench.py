@@ -34,6 +34,10 @@ METRIC = "Gcell-updates/s fwd & FWI grad at 512²×128 shots; % HBM peak; vs pla
 UNIT = "Gcell-updates/s"
 FWD_BYTES_PER_CELL = 12.0    # read u, read u_old, write u_next (float32)
 GRAD_BYTES_PER_CELL = 28.0   # forward 12 + adjoint 12 + one read of the forward field 4
+# DRAM bytes (read + write) of one forward launch at 512^2 x 128 shots, by launch shape
+# (rows per lane, warps, steps per launch), from one ncu capture of that launch
+# (profiles/tb_kernel_fwd_512x512x128.md)
+FWD_TRAFFIC = {(4, 32, 15): 332.569856e6 + 248.594176e6}
 
 
 def peaks():
@@ -241,6 +245,7 @@ def bench_gradient(args, acq, medium, rx, waves, observed, tuning, device, world
                   "rel_l2_fused_vs_plain": agree},
         "e2e": {"value": acq.cell_updates * world / e2e_s / 1e9, "unit": UNIT,
                 "h2d_bytes_per_step": int(m_host.size * 8), "d2h_bytes_per_step": int(n * n * 8)},
+        "tuning": plan.tuning,
         "gpu_launches_per_step": 3 * launches + 2,
         "workspace_gib": plan.workspace_bytes / 2 ** 30,
     }
@@ -274,12 +279,15 @@ def run_ours(args):
     rx = acq.ring.receiver_taps()
     waves = torch.as_tensor(acq.wavelet[None], dtype=torch.float32, device=device)
     if args.tuning:
-        tuning = json.loads(args.tuning)
+        tuning = grad_tuning = json.loads(args.tuning)
     else:
         from soundwavesimulation_gb300.autotune import autotune
         t_tune = time.perf_counter()
         tuning = autotune(medium, rx, acq.source_tables(), waves, nt, verbose=rank == 0)
-        print(f"autotune {time.perf_counter() - t_tune:.1f} s -> {tuning}", file=sys.stderr)
+        grad_tuning = autotune(medium, rx, acq.source_tables(), waves, nt, verbose=rank == 0,
+                               for_gradient=True)
+        print(f"autotune {time.perf_counter() - t_tune:.1f} s -> forward {tuning}, gradient {grad_tuning}",
+              file=sys.stderr)
     plan = FusedPlan(medium, rx, acq.source_tables(), waves, nt, tuning=tuning)
     traces = torch.empty((S, acq.n_elements, nt), dtype=torch.float32, device=device)
     launches_per_pass = math.ceil(nt / plan.tuning["steps_per_launch"])
@@ -351,11 +359,14 @@ def run_ours(args):
     d2h = int(host_traces.numel()) * 4
 
     # ---- FWI gradient, same grid and shots: forward with checkpoints + residual + adjoint
-    grad = bench_gradient(args, acq, medium, rx, waves, traces, tuning, device, world, barrier,
+    grad = bench_gradient(args, acq, medium, rx, waves, traces, grad_tuning, device, world, barrier,
                           solver, sampler, tr)
 
     hbm, peak_kind = peaks()
     achieved = FWD_BYTES_PER_CELL * acq.cell_updates / (ms * 1e-3) / 1e9
+    launch_us = ms * 1e3 / launches_per_pass
+    shape = (plan.tuning["rows_per_lane"], plan.tuning["warps"], plan.tuning["steps_per_launch"])
+    traffic = FWD_TRAFFIC.get(shape) if (n, S) == (512, 128) else None
     out = None
     if rank == 0:
         cpu_v, cpu_s = cpu_sample(acq)
@@ -368,9 +379,12 @@ def run_ours(args):
                        "grid": [n, n], "shots": S, "steps": nt, "receivers": acq.n_elements,
                        "tuning": plan.tuning, "l2": "working set 256 MiB > L2 (no flush needed)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
+                         "frac": achieved / hbm, "traffic": traffic, "launch_us": launch_us,
+                         "dram_frac": (traffic / (launch_us * 1e-6) / 1e9 / hbm) if traffic else None,
                          "note": f"12 B per cell-update algorithmic; peak {peak_kind}; temporal blocking "
-                                 "makes the algorithmic fraction exceed the single-step roofline"},
+                                 "makes the algorithmic fraction exceed the single-step roofline; traffic = "
+                                 "ncu dram bytes read+written per launch for this launch shape "
+                                 "(profiles/tb_kernel_fwd_512x512x128.md), dram_frac = traffic / launch_us / peak"},
             "plain": {"value": plain_value, "unit": UNIT, "shots_sampled": plain_shots,
                       "speedup": value / world / plain_value, "bitwise_equal_traces": same},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

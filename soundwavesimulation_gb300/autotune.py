@@ -30,11 +30,17 @@ def candidates(shapes=SHAPES, depths=DEPTHS):
 
 
 def autotune(medium, receivers, sources, waveforms, n_steps, launches=3, repeats=2, shapes=SHAPES,
-             depths=DEPTHS, verbose=False):
-    """Fastest tuning dict for this acquisition; probes ``launches`` temporal blocks per shape."""
+             depths=DEPTHS, verbose=False, for_gradient=False):
+    """Fastest tuning dict for this acquisition; probes ``launches`` temporal blocks per shape.
+
+    With ``for_gradient`` each probe is a whole gradient pass (forward with
+    checkpoints, recompute and adjoint launches), since the adjoint kernel
+    prefers other shapes than the forward (its coefficient tile is read
+    through L1, so its shared-memory footprint matters).
+    """
     dev = medium.device
     n_shots = len(sources[0])
-    key = (medium.ny, medium.nx, n_shots, len(receivers[0]), str(dev), shapes, depths)
+    key = (medium.ny, medium.nx, n_shots, len(receivers[0]), str(dev), shapes, depths, bool(for_gradient))
     if key in _CACHE:
         return dict(_CACHE[key])
     best, best_rate, report = None, 0.0, []
@@ -42,16 +48,29 @@ def autotune(medium, receivers, sources, waveforms, n_steps, launches=3, repeats
     for cand in candidates(shapes, depths):
         steps = min(int(n_steps), launches * cand["steps_per_launch"])
         try:
-            plan = FusedPlan(medium, receivers, sources, waveforms, steps, tuning=cand)
+            plan = FusedPlan(medium, receivers, sources, waveforms, steps, tuning=cand,
+                             for_gradient=for_gradient)
         except ValueError:
             continue  # shape not supported for this grid (tiling or shared memory)
         traces = plan.forward()
+        grad = None
+        if for_gradient:
+            grad = torch.zeros((medium.ny, medium.pitch), dtype=torch.float64, device=dev)
+
+        def one_pass():
+            if for_gradient:
+                plan.forward(traces, save_checkpoints=True)
+                plan.adjoint(traces, grad)  # any residual: the cost does not depend on its values
+            else:
+                plan.forward(traces)
+
+        one_pass()
         torch.cuda.synchronize(dev)
         stream = torch.cuda.current_stream(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(repeats):
-            plan.forward(traces)
+            one_pass()
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / repeats
@@ -59,7 +78,7 @@ def autotune(medium, receivers, sources, waveforms, n_steps, launches=3, repeats
         report.append((rate, cand))
         if rate > best_rate:
             best, best_rate = dict(cand), rate
-        del plan, traces
+        del plan, traces, grad
     if best is None:
         raise RuntimeError("no candidate launch shape fits this problem")
     if verbose:
