@@ -19,7 +19,7 @@ from .engine import FusedPlan
 
 _CACHE: dict = {}
 
-SHAPES = ((8, 16), (8, 12), (4, 32), (4, 16))   # (rows per lane, warps)
+SHAPES = ((8, 16), (8, 12), (8, 10), (4, 32), (4, 16))   # (rows per lane, warps)
 DEPTHS = (6, 8, 10, 12, 15, 19, 23)              # steps per launch
 
 

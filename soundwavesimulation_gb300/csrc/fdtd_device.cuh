@@ -127,6 +127,7 @@ struct TbParams {
   const int* rxl;
   const TbRec* recs;
   int nrow_max, nrxl_max, tmax;  // nrow_max: staged tap rows of the largest tile
+  int adj_coef;          // adjoint: 1 = coefficient tile in shared memory, 0 = read through L1
   // sources
   const SrcNode* src;    // (nshots, SRC_MAX)
   const int* nsrc;       // (nshots)
@@ -160,16 +161,21 @@ struct TbSmem {
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
 
 __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int nrow_max,
-                                                 int nrxl_max, int tmax) {
+                                                 int nrxl_max, int tmax, int adj_coef) {
   TbSmem m;
   const size_t region = size_t(nw) * ky * RX * sizeof(float);
   size_t off = 0;
-  // forward / recompute keep the region's coefficients in shared memory; the
-  // adjoint reads them through L1 and uses the space to stream in the next
-  // step's Laplacian tile (cp.async) instead
+  // every mode keeps the region's coefficients in shared memory, except an
+  // adjoint whose launch shape leaves no room (adj_coef = 0): it reads them
+  // through L1 and shares the space with the next step's Laplacian tile, which
+  // the adjoint streams in with cp.async
   m.coef = off;
   m.lap = off;
   off += region;
+  if (mode == MODE_ADJ && adj_coef) {
+    m.lap = off;
+    off += region;
+  }
   m.g = off; if (mode == MODE_ADJ) off += region;
   m.xch = off; off += size_t(2) * nw * 2 * 32 * 16;
   // tap stage: per step, the full 4-cell row of every (thread, band row) that holds

@@ -106,6 +106,7 @@ struct fdtd_plan {
   std::vector<SrcNode> src;
   std::vector<int> nsrc;
   int nrow_max = 0, nrxl_max = 0;
+  int adj_coef = 0;
   int ckpt_every = 0, nseg = 1;
   size_t field_elems = 0;
   // workspace offsets
@@ -153,6 +154,7 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.rxl = reinterpret_cast<const int*>(p->ws + p->o_rxl);
   q.recs = reinterpret_cast<const TbRec*>(p->ws + p->o_recs);
   q.nrow_max = p->nrow_max;
+  q.adj_coef = p->adj_coef;
   q.nrxl_max = p->nrxl_max;
   q.tmax = p->tmax;
   q.src = reinterpret_cast<const SrcNode*>(p->ws + p->o_src);
@@ -575,8 +577,10 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   p->tun = t;
   rc = build_tables(p, problem);
   if (rc) { delete p; return rc; }
+  // the adjoint keeps its coefficient tile in shared memory when that fits
+  p->adj_coef = tb_smem_layout(p->nw, p->ky, MODE_ADJ, p->nrow_max, p->nrxl_max, p->tmax, 1).total <= SMEM_LIMIT;
   for (int m = 0; m < 3; ++m) {
-    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->nrow_max, p->nrxl_max, p->tmax).total;
+    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->nrow_max, p->nrxl_max, p->tmax, p->adj_coef).total;
     if (p->smem[m] > SMEM_LIMIT && (m == MODE_FWD || for_gradient)) {
       delete p;
       return fail(FDTD_ERR_UNSUPPORTED, "shared memory need exceeds 227 KB; use fewer steps per launch or warps");

@@ -74,11 +74,11 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Coefficients (c dt)^2 of band row r: from the shared-memory copy of the region
-// (forward, recompute) or through L1 from global memory (adjoint); zero outside
-// the domain.
+// or, for an adjoint without room for it, through L1 from global memory; zero
+// outside the domain.
 template <int MODE>
 __device__ __forceinline__ float4 coefrow(const TbParams& p, const Ctx& x, const float4* coef4, int r) {
-  if (MODE != MODE_ADJ) return coef4[r * 32];
+  if (MODE != MODE_ADJ || p.adj_coef) return coef4[r * 32];
   if (!((x.rowvalid >> r) & 1u)) return make_float4(0.f, 0.f, 0.f, 0.f);
   return ldg4(x.gcoef + (long long)r * p.pitch);
 }
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = p.nwarps;
   const int nthr = nw * 32;
-  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax);
+  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef);
   Ctx x;
   x.tid = threadIdx.x;
   x.w = x.tid >> 5;
@@ -501,14 +501,15 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
     }
 
     // coefficients of the region (zero outside the domain; the padding columns of
-    // coef are zero in memory) or, for the adjoint, a cleared gradient tile
+    // coef are zero in memory) and, for the adjoint, a cleared gradient tile
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
-      if (MODE != MODE_ADJ) {
+      if (MODE != MODE_ADJ || p.adj_coef) {
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if ((x.rowvalid >> r) & 1u) v = ldg4(x.gcoef + (long long)r * p.pitch);
         reinterpret_cast<float4*>(x.s_coef)[(x.w * KY + r) * 32 + x.lane] = v;
-      } else {
+      }
+      if (MODE == MODE_ADJ) {
         reinterpret_cast<float4*>(x.s_g)[(x.w * KY + r) * 32 + x.lane] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
