@@ -77,7 +77,6 @@ constexpr int MODE_REC = 1;  // recompute: sources in, Laplacian of every step o
 constexpr int MODE_ADJ = 2;  // adjoint: residual in, imaging into the gradient
 
 constexpr int RX = 128;       // region width: 32 lanes x 4 columns
-constexpr int SRC_MAX = 8;    // injection nodes per shot
 constexpr int TAP_C = 8;      // receivers sharing one tap node
 constexpr int SRC_C = 4;      // source entries sharing one node
 
@@ -114,6 +113,13 @@ struct SrcNode {         // one injection node of one shot
   float w[SRC_C];
 };
 
+struct SrcTap {          // one injection node of one shot inside one tile
+  int packed;            // (thread << 8) | (row_in_lane * 4 + column_in_lane)
+  int srow;              // staged source row (its float is srow * 4 + column)
+  int node;              // index into the shot's node list
+  int pad;
+};
+
 struct TbParams {
   // grid
   int ny, nx, pitch;
@@ -129,8 +135,11 @@ struct TbParams {
   int nrow_max, nrxl_max, tmax;  // nrow_max: staged tap rows of the largest tile
   int adj_coef;          // adjoint: 1 = coefficient tile in shared memory, 0 = read through L1
   // sources
-  const SrcNode* src;    // (nshots, SRC_MAX)
-  const int* nsrc;       // (nshots)
+  const SrcNode* src;    // (nshots, nsrc_max) merged injection nodes
+  int nsrc_max;
+  const SrcTap* stap;    // nodes per (shot, tile), sorted by (thread, row, column)
+  const int* stap_off;   // (nshots * ntiles + 1) offsets into stap
+  int nsrow_max;         // staged source rows of the largest (shot, tile)
   const float* waveforms;
   int wave_len;
   // state (nshots, ny, pitch)
@@ -155,13 +164,13 @@ struct TbParams {
 // Dynamic shared-memory carve-up of the temporally blocked kernel; the host
 // sizes the launch with the same function.
 struct TbSmem {
-  size_t coef, lap, g, xch, tap, res, src, mask, base, srcpos, total;
+  size_t coef, lap, g, xch, tap, res, src, mask, base, smask, sbase, total;
 };
 
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
 
 __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int nrow_max,
-                                                 int nrxl_max, int tmax, int adj_coef) {
+                                                 int nrxl_max, int tmax, int adj_coef, int nsrow_max) {
   TbSmem m;
   const size_t region = size_t(nw) * ky * RX * sizeof(float);
   size_t off = 0;
@@ -183,10 +192,13 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
   // where a row's cell has no tap)
   m.tap = off; off += size_t(tmax) * (nrow_max > 0 ? nrow_max : 1) * 4 * sizeof(float);
   m.res = off; if (mode == MODE_ADJ) off += tb_align16(size_t(nrxl_max > 0 ? nrxl_max : 1) * tmax * sizeof(float));
-  m.src = off; off += tb_align16(size_t(tmax) * SRC_MAX * sizeof(float));
+  // source stage: per step, the 4-cell rows holding this shot's injection nodes
+  // (forward and recompute only)
+  m.src = off; if (mode != MODE_ADJ) off += size_t(tmax) * (nsrow_max > 0 ? nsrow_max : 1) * 4 * sizeof(float);
   m.mask = off; off += size_t(nw) * 32 * sizeof(unsigned);
   m.base = off; off += size_t(nw) * 32 * sizeof(int);
-  m.srcpos = off; off += SRC_MAX * sizeof(int);
+  m.smask = off; off += size_t(nw) * 32 * sizeof(unsigned);
+  m.sbase = off; off += size_t(nw) * 32 * sizeof(int);
   m.total = tb_align16(off);
   return m;
 }

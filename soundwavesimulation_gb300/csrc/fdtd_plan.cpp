@@ -103,14 +103,17 @@ struct fdtd_plan {
   std::vector<TbTap> taps;
   std::vector<int> rxl;
   std::vector<TbRec> recs;
-  std::vector<SrcNode> src;
+  std::vector<SrcNode> src;       // (n_shots, nsrc_max) merged nodes
   std::vector<int> nsrc;
+  std::vector<SrcTap> stap;       // per (shot, tile) nodes inside the region
+  std::vector<int> stap_off;      // (n_shots * n_tiles + 1)
+  int nsrc_max = 1, nsrow_max = 0;
   int nrow_max = 0, nrxl_max = 0;
   int adj_coef = 0;
   int ckpt_every = 0, nseg = 1;
   size_t field_elems = 0;
   // workspace offsets
-  size_t o_tiles = 0, o_taps = 0, o_rxl = 0, o_recs = 0, o_src = 0, o_nsrc = 0;
+  size_t o_tiles = 0, o_taps = 0, o_rxl = 0, o_recs = 0, o_src = 0, o_stap = 0, o_stap_off = 0;
   size_t o_state[2][2] = {{0, 0}, {0, 0}};
   size_t o_adj[2][2] = {{0, 0}, {0, 0}};
   size_t o_ckpt = 0, ckpt_elem_bytes = 4, o_scales = 0, o_seg = 0;
@@ -158,7 +161,10 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.nrxl_max = p->nrxl_max;
   q.tmax = p->tmax;
   q.src = reinterpret_cast<const SrcNode*>(p->ws + p->o_src);
-  q.nsrc = reinterpret_cast<const int*>(p->ws + p->o_nsrc);
+  q.nsrc_max = p->nsrc_max;
+  q.stap = reinterpret_cast<const SrcTap*>(p->ws + p->o_stap);
+  q.stap_off = reinterpret_cast<const int*>(p->ws + p->o_stap_off);
+  q.nsrow_max = p->nsrow_max;
   q.waveforms = p->prob.src.waveforms;
   q.wave_len = p->prob.src.waveform_len;
   q.nrx = p->prob.rx.n;
@@ -307,38 +313,77 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
 
   // per-shot injection nodes, duplicates merged in entry order
   const int S = prob->n_shots, K = prob->src.per_shot;
-  p->src.assign((size_t)S * SRC_MAX, SrcNode());
-  p->nsrc.assign(S, 0);
+  std::vector<std::vector<SrcNode>> shot_nodes(S);
   for (int s = 0; s < S; ++s) {
-    int cnt = 0;
+    std::map<std::pair<int, int>, int> where;
+    auto& list = shot_nodes[s];
     for (int j = 0; j < K; ++j) {
       const int e = s * K + j;
       if (prob->src.wave[e] < 0) continue;
       const int row = prob->src.row[e], col = prob->src.col[e];
       if (row < 0 || row >= ny || col < 0 || col >= nx) return fail(FDTD_ERR_INVALID, "source outside the grid");
       if (prob->src.wave[e] >= prob->src.n_waves) return fail(FDTD_ERR_INVALID, "source waveform index out of range");
-      int found = -1;
-      for (int m = 0; m < cnt; ++m) {
-        const SrcNode& sn = p->src[(size_t)s * SRC_MAX + m];
-        if (sn.row == row && sn.col == col) found = m;
-      }
-      if (found < 0) {
-        if (cnt >= SRC_MAX) return fail(FDTD_ERR_UNSUPPORTED, "more than 8 source nodes in one shot");
-        SrcNode& sn = p->src[(size_t)s * SRC_MAX + cnt];
+      auto it = where.find({row, col});
+      int found;
+      if (it == where.end()) {
+        SrcNode sn;
         sn.row = row;
         sn.col = col;
         for (int q = 0; q < SRC_C; ++q) { sn.wave[q] = -1; sn.w[q] = 0.f; }
-        found = cnt++;
+        found = (int)list.size();
+        where[{row, col}] = found;
+        list.push_back(sn);
+      } else {
+        found = it->second;
       }
-      SrcNode& sn = p->src[(size_t)s * SRC_MAX + found];
+      SrcNode& sn = list[found];
       int q = 0;
       while (q < SRC_C && sn.wave[q] >= 0) ++q;
       if (q == SRC_C) return fail(FDTD_ERR_UNSUPPORTED, "more than 4 source entries on one node");
       sn.wave[q] = prob->src.wave[e];
       sn.w[q] = prob->src.w[e];
     }
-    p->nsrc[s] = cnt;
   }
+  p->nsrc_max = 1;
+  for (int s = 0; s < S; ++s) p->nsrc_max = std::max(p->nsrc_max, (int)shot_nodes[s].size());
+  p->src.assign((size_t)S * p->nsrc_max, SrcNode());
+  p->nsrc.assign(S, 0);
+  for (int s = 0; s < S; ++s) {
+    p->nsrc[s] = (int)shot_nodes[s].size();
+    std::copy(shot_nodes[s].begin(), shot_nodes[s].end(), p->src.begin() + (size_t)s * p->nsrc_max);
+  }
+  // per (shot, tile): the nodes inside the region, sorted by (thread, row, column);
+  // every (thread, band row) holding one is a staged source row
+  const int NT = (int)p->tiles.size();
+  p->stap.clear();
+  p->stap_off.assign((size_t)S * NT + 1, 0);
+  p->nsrow_max = 0;
+  for (int s = 0; s < S; ++s) {
+    for (int ti = 0; ti < NT; ++ti) {
+      const TbTile& t = p->tiles[ti];
+      p->stap_off[(size_t)s * NT + ti] = (int)p->stap.size();
+      std::vector<std::pair<int, int>> local;  // (packed, node)
+      for (int j = 0; j < p->nsrc[s]; ++j) {
+        const SrcNode& sn = shot_nodes[s][j];
+        const int ly = sn.row - t.ry0, lx = sn.col - t.rx0;
+        if (ly < 0 || ly >= RY || lx < 0 || lx >= RX) continue;
+        local.push_back({(((ly / KY) * 32 + (lx >> 2)) << 8) | ((ly % KY) * 4 + (lx & 3)), j});
+      }
+      std::sort(local.begin(), local.end());
+      int nrow = 0;
+      for (size_t i = 0; i < local.size(); ++i) {
+        if (i == 0 || (local[i].first >> 2) != (local[i - 1].first >> 2)) ++nrow;
+        SrcTap st;
+        st.packed = local[i].first;
+        st.srow = nrow - 1;
+        st.node = local[i].second;
+        st.pad = 0;
+        p->stap.push_back(st);
+      }
+      p->nsrow_max = std::max(p->nsrow_max, nrow);
+    }
+  }
+  p->stap_off[(size_t)S * NT] = (int)p->stap.size();
   return FDTD_OK;
 }
 
@@ -578,9 +623,9 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   rc = build_tables(p, problem);
   if (rc) { delete p; return rc; }
   // the adjoint keeps its coefficient tile in shared memory when that fits
-  p->adj_coef = tb_smem_layout(p->nw, p->ky, MODE_ADJ, p->nrow_max, p->nrxl_max, p->tmax, 1).total <= SMEM_LIMIT;
+  p->adj_coef = tb_smem_layout(p->nw, p->ky, MODE_ADJ, p->nrow_max, p->nrxl_max, p->tmax, 1, p->nsrow_max).total <= SMEM_LIMIT;
   for (int m = 0; m < 3; ++m) {
-    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->nrow_max, p->nrxl_max, p->tmax, p->adj_coef).total;
+    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->nrow_max, p->nrxl_max, p->tmax, p->adj_coef, p->nsrow_max).total;
     if (p->smem[m] > SMEM_LIMIT && (m == MODE_FWD || for_gradient)) {
       delete p;
       return fail(FDTD_ERR_UNSUPPORTED, "shared memory need exceeds 227 KB; use fewer steps per launch or warps");
@@ -596,7 +641,8 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   p->o_rxl = off; off = align_up(off + std::max<size_t>(1, p->rxl.size()) * sizeof(int));
   p->o_recs = off; off = align_up(off + std::max<size_t>(1, p->recs.size()) * sizeof(TbRec));
   p->o_src = off; off = align_up(off + p->src.size() * sizeof(SrcNode));
-  p->o_nsrc = off; off = align_up(off + p->nsrc.size() * sizeof(int));
+  p->o_stap = off; off = align_up(off + std::max<size_t>(1, p->stap.size()) * sizeof(SrcTap));
+  p->o_stap_off = off; off = align_up(off + p->stap_off.size() * sizeof(int));
   for (int s = 0; s < 2; ++s)
     for (int f = 0; f < 2; ++f) { p->o_state[s][f] = off; off = align_up(off + fb); }
   if (p->for_gradient) {
@@ -649,7 +695,8 @@ int32_t fdtd_plan_bind(fdtd_plan* p, void* workspace, size_t bytes, void* stream
       {p->o_rxl, p->rxl.data(), p->rxl.size() * sizeof(int)},
       {p->o_recs, p->recs.data(), p->recs.size() * sizeof(TbRec)},
       {p->o_src, p->src.data(), p->src.size() * sizeof(SrcNode)},
-      {p->o_nsrc, p->nsrc.data(), p->nsrc.size() * sizeof(int)},
+      {p->o_stap, p->stap.data(), p->stap.size() * sizeof(SrcTap)},
+      {p->o_stap_off, p->stap_off.data(), p->stap_off.size() * sizeof(int)},
   };
   for (const Up& u : ups) {
     if (!u.n) continue;

@@ -36,17 +36,16 @@ struct Ctx {
   int rx0, ry0, flags;
   int y0, xb;               // global row of this thread's r = 0, column of c = 0
   unsigned own_rows, own_cols;
-  unsigned mask, srcsel;
+  unsigned mask, smask;     // band rows holding receiver taps / source nodes
   unsigned rowvalid;        // band rows inside the domain (adjoint coefficient loads)
-  int base;
+  int base, sbase;          // first staged tap row / source row of this thread
   const float* gcoef;       // global coefficients at (y0, xb) (adjoint)
   float* s_coef;
   float* s_lap;
   float* s_g;
   float4* s_xch;
   float* s_tap;
-  const float* s_src;
-  const int* s_srcpos;
+  float* s_src;
 };
 
 // Stencil operand of one band row: the field itself in every mode (the adjoint
@@ -307,15 +306,20 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
 
   // ---- injection before the boundary update
   if (MODE != MODE_ADJ) {
-    unsigned sel = x.srcsel;
-    while (sel) {
-      const int j = __ffs(sel) - 1;
-      sel &= sel - 1u;
-      const int bit = x.s_srcpos[j] & 255;
-      const float v = x.s_src[k * SRC_MAX + j];
+    if (x.smask) {
+      // source injection: whole staged rows, zero where a cell holds no node
+      const float4* inj = reinterpret_cast<const float4*>(x.s_src) + k * p.nsrow_max + x.sbase;
+      int slot = 0;
 #pragma unroll
-      for (int b = 0; b < 4 * KY; ++b) {
-        if (b == bit) P[b >> 2][b & 3] = inj_add(P[b >> 2][b & 3], v);
+      for (int r = 0; r < KY; ++r) {
+        if ((x.smask >> r) & 1u) {
+          const float4 v = inj[slot];
+          P[r][0] = inj_add(P[r][0], v.x);
+          P[r][1] = inj_add(P[r][1], v.y);
+          P[r][2] = inj_add(P[r][2], v.z);
+          P[r][3] = inj_add(P[r][3], v.w);
+          ++slot;
+        }
       }
     }
   } else if (x.mask) {
@@ -428,7 +432,6 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
       }
     }
   }
-  const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
   x.s_xch[x.w * 64 + x.lane] = opval(C[0]);
   x.s_xch[x.w * 64 + 32 + x.lane] = opval(C[KY - 1]);
   if (MODE == MODE_ADJ && x.own_rows && x.own_cols && p.n0 >= 1) prefetch_lap<KY>(p, x, p.n0);
@@ -450,7 +453,7 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = p.nwarps;
   const int nthr = nw * 32;
-  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef);
+  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef, p.nsrow_max);
   Ctx x;
   x.tid = threadIdx.x;
   x.w = x.tid >> 5;
@@ -462,13 +465,11 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   x.s_xch = reinterpret_cast<float4*>(smem + L.xch);
   x.s_tap = reinterpret_cast<float*>(smem + L.tap);
   float* s_res = reinterpret_cast<float*>(smem + L.res);
-  float* s_src = reinterpret_cast<float*>(smem + L.src);
   unsigned* s_mask = reinterpret_cast<unsigned*>(smem + L.mask);
   int* s_base = reinterpret_cast<int*>(smem + L.base);
-  int* s_srcpos = reinterpret_cast<int*>(smem + L.srcpos);
-  x.s_src = s_src;
-  x.s_srcpos = s_srcpos;
-  const int RY = nw * KY;
+  unsigned* s_smask = reinterpret_cast<unsigned*>(smem + L.smask);
+  int* s_sbase = reinterpret_cast<int*>(smem + L.sbase);
+  x.s_src = reinterpret_cast<float*>(smem + L.src);
   const int nitems = p.ntiles * p.nshots;
 
   // Items are (tile, shot) pairs with shots varying fastest, dealt out with a
@@ -515,35 +516,20 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
     }
     s_mask[x.tid] = 0u;
     s_base[x.tid] = 0x7fffffff;
-    if (x.tid < SRC_MAX) {
-      int pos = -1;
-      if (MODE != MODE_ADJ && x.tid < p.nsrc[s]) {
-        const SrcNode sn = p.src[s * SRC_MAX + x.tid];
-        const int ly = sn.row - t.ry0, lx = sn.col - t.rx0;
-        if (ly >= 0 && ly < RY && lx >= 0 && lx < RX) {
-          pos = (((ly / KY) * 32 + (lx >> 2)) << 8) | ((ly % KY) * 4 + (lx & 3));
-        }
+    s_smask[x.tid] = 0u;
+    s_sbase[x.tid] = 0x7fffffff;
+    // this shot's injection nodes inside the region (sorted by thread, row, column)
+    const int so = (MODE != MODE_ADJ) ? __ldg(p.stap_off + s * p.ntiles + ti) : 0;
+    const int ns = (MODE != MODE_ADJ) ? __ldg(p.stap_off + s * p.ntiles + ti + 1) - so : 0;
+    if (MODE != MODE_ADJ && ns > 0) {
+      // staged source rows start at zero: cells without a node add nothing
+      const int nrows = p.stap[so + ns - 1].srow + 1;
+      for (int i = x.tid; i < p.nsteps * nrows; i += nthr) {
+        const int k = i / nrows, j = i - k * nrows;
+        reinterpret_cast<float4*>(x.s_src)[k * p.nsrow_max + j] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      s_srcpos[x.tid] = pos;
     }
-    if (MODE != MODE_ADJ) {
-      for (int i = x.tid; i < p.nsteps * SRC_MAX; i += nthr) {
-        const int k = i / SRC_MAX, j = i - k * SRC_MAX;
-        float acc = 0.f;
-        if (j < p.nsrc[s]) {
-          const SrcNode sn = p.src[s * SRC_MAX + j];
-          const int nstep = p.n0 + k;
-#pragma unroll
-          for (int q = 0; q < SRC_C; ++q) {
-            if (sn.wave[q] >= 0) {
-              const float v = (nstep < p.wave_len) ? __ldg(p.waveforms + (long long)sn.wave[q] * p.wave_len + nstep) : 0.f;
-              acc = inj_acc(acc, sn.w[q], v);
-            }
-          }
-        }
-        s_src[i] = acc;
-      }
-    } else {
+    if (MODE == MODE_ADJ) {
       // staged injection rows start at zero: cells without a tap add nothing
       for (int i = x.tid; i < p.nsteps * t.nrow; i += nthr) {
         const int k = i / t.nrow, j = i - k * t.nrow;
@@ -556,11 +542,32 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
       }
     }
     __syncthreads();
-    // per thread: which band rows hold tap nodes, and the first staged row
+    // per thread: which band rows hold tap nodes / source nodes, and the first
+    // staged row of each; the source values of every step go to the stage
     for (int i = x.tid; i < t.ntap; i += nthr) {
       const TbTap& tp = p.taps[t.tap_off + i];
       atomicOr(&s_mask[tp.packed >> 8], 1u << ((tp.packed & 255) >> 2));
       atomicMin(&s_base[tp.packed >> 8], tp.srow);
+    }
+    for (int i = x.tid; i < ns; i += nthr) {
+      const SrcTap st = p.stap[so + i];
+      atomicOr(&s_smask[st.packed >> 8], 1u << ((st.packed & 255) >> 2));
+      atomicMin(&s_sbase[st.packed >> 8], st.srow);
+    }
+    for (int i = x.tid; i < ns * p.nsteps; i += nthr) {
+      const int e = i / p.nsteps, k = i - e * p.nsteps;
+      const SrcTap st = p.stap[so + e];
+      const SrcNode sn = p.src[(long long)s * p.nsrc_max + st.node];
+      const int nstep = p.n0 + k;
+      float acc = 0.f;
+#pragma unroll
+      for (int q = 0; q < SRC_C; ++q) {
+        if (sn.wave[q] >= 0) {
+          const float v = (nstep < p.wave_len) ? __ldg(p.waveforms + (long long)sn.wave[q] * p.wave_len + nstep) : 0.f;
+          acc = inj_acc(acc, sn.w[q], v);
+        }
+      }
+      x.s_src[(k * p.nsrow_max + st.srow) * 4 + (st.packed & 3)] = acc;
     }
     __syncthreads();
     if (MODE == MODE_ADJ) {
@@ -582,14 +589,8 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
     }
     x.mask = s_mask[x.tid];
     x.base = s_base[x.tid];
-    x.srcsel = 0;
-    if (MODE != MODE_ADJ) {
-#pragma unroll
-      for (int j = 0; j < SRC_MAX; ++j) {
-        const int pos = s_srcpos[j];
-        if (pos >= 0 && (pos >> 8) == x.tid) x.srcsel |= 1u << j;
-      }
-    }
+    x.smask = s_smask[x.tid];
+    x.sbase = s_sbase[x.tid];
     // run_item publishes the exchange rows and synchronises before the first step
 
     if (t.flags) {

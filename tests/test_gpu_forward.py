@@ -205,3 +205,32 @@ def test_fused_engine_shapes_and_tunings(tb, ny, nx, shots, nt, tuning):
         ref += tr
     del q
     assert rel(traces, ref) < TRACE_TOL
+
+
+@pytest.mark.parametrize("tuning", [{"steps_per_launch": 6, "rows_per_lane": 4, "warps": 16},
+                                    {"steps_per_launch": 13}])
+def test_fused_many_sources_per_shot(tb, tuning):
+    """Focused-arc style shots: 40 injection nodes per shot with three waveforms
+    (2DArcFDTD.py:203-228 fires every transmit element with its own delayed
+    waveform), two entries sharing one node, nodes spread over several tiles."""
+    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan
+    ny, nx, S, K, nt = 140, 170, 2, 40, 70
+    p = _random_problem(ny, nx, S, 30, nt, seed=77, per_shot=K)
+    rng = np.random.default_rng(5)
+    wave_idx = rng.integers(0, 3, size=(S, K))
+    p["srow"][:, 1] = p["srow"][:, 0]
+    p["scol"][:, 1] = p["scol"][:, 0]
+    waves = np.concatenate([p["waves"], -0.5 * p["waves"][:1]])
+    medium = DeviceMedium(p["c"], p["dx"], p["dy"], p["dt"], "cuda")
+    plan = FusedPlan(medium, (p["row0"], p["col0"], p["w"]), (p["srow"], p["scol"], p["sw"], wave_idx),
+                     torch.as_tensor(waves, dtype=torch.float32, device="cuda"), nt, tuning=tuning)
+    traces = plan.forward().cpu().numpy()
+    geo = {"row0": p["row0"], "col0": p["col0"], "row1": p["row0"] + 1, "col1": p["col0"] + 1,
+           "w00": p["w"][:, 0], "w10": p["w"][:, 1], "w01": p["w"][:, 2], "w11": p["w"][:, 3]}
+    ref = np.zeros(traces.shape)
+    for k in range(3):  # the engine is linear in the sources: one oracle run per waveform
+        fields = orc.point_sources((ny, nx), p["srow"], p["scol"], p["sw"] * (wave_idx == k))
+        values = np.repeat(waves[k][None], S, axis=0)
+        tr, _, _, _ = orc.simulate_shots_batch(p["c"], p["dx"], p["dy"], p["dt"], geo, fields, values, nt)
+        ref += tr
+    assert rel(traces, ref) < TRACE_TOL
