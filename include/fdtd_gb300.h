@@ -275,6 +275,26 @@ int32_t fdtd_forward_plain_static(const fdtd_problem* problem, float* traces, vo
 int32_t fdtd_tile_axis(int32_t n, int32_t region, int32_t align, int32_t halo,
                        int32_t band, int32_t max_tiles, int32_t* out, int32_t* n_tiles);
 
+/* ------------------------------------------------- inversion helpers */
+
+/* Adds the Tikhonov (1/2 alpha ||grad m||^2) and smoothed total-variation
+   (tv sum(sqrt(|grad m|^2 + tv_eps^2) - tv_eps)) gradients of the slowness squared
+   m (float64 (ny, nx), device) into `grad` on the mask (uint8, non-zero = inside)
+   and sets grad to 0 outside it; adds both values into the device double `value`.
+   Replaces tikhonov / total_variation (fdtd2d/inversion/misfit.py:19-71) and the
+   host gradient assembly of misfit_and_grad (invert_ring.py:655-659). */
+int32_t fdtd_regularization(int32_t ny, int32_t nx, const double* m, const uint8_t* mask, double alpha,
+                            double tv, double tv_eps, double* grad, double* value, void* stream);
+/* m = clip(m, m_min, m_max) inside the mask, m_exterior outside
+   (TorchLeastSquaresFWI.project, invert_ring.py:559-565). */
+int32_t fdtd_project(int64_t n, double* m, const uint8_t* mask, double m_min, double m_max,
+                     double m_exterior, void* stream);
+/* One projected Adam step on the mask (invert_ring.py:842-853), iteration >= 1;
+   first / second are the moment arrays (zero before the first step). */
+int32_t fdtd_adam_step(int64_t n, double* m, const double* grad, const uint8_t* mask, double* first,
+                       double* second, double learning_rate, double beta1, double beta2, double epsilon,
+                       int32_t iteration, double m_min, double m_max, double m_exterior, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,6 +69,12 @@ _SIGNATURES = {
     "fdtd_plan_workspace_bytes": (c_int32, [c_void_p, POINTER(c_size_t)]),
     "fdtd_plan_tuning": (c_int32, [c_void_p, POINTER(Tuning)]),
     "fdtd_plan_bind": (c_int32, [c_void_p, c_void_p, c_size_t, c_void_p]),
+    "fdtd_regularization": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_double, c_double, c_double,
+                                      c_void_p, c_void_p, c_void_p]),
+    "fdtd_project": (c_int32, [ctypes.c_int64, c_void_p, c_void_p, c_double, c_double, c_double, c_void_p]),
+    "fdtd_adam_step": (c_int32, [ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_double,
+                                 c_double, c_double, c_double, c_int32, c_double, c_double, c_double,
+                                 c_void_p]),
     "fdtd_plan_set_medium": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "fdtd_forward": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
     "fdtd_adjoint": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),

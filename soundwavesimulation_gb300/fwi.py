@@ -28,6 +28,7 @@ import torch
 from . import _lib
 from .engine import FusedPlan, chain_rule, residual_misfit
 from .medium import c_from_m, m_from_c, tikhonov, total_variation
+from .optim import project_device, regularization_device
 from .torch_backend import TorchFDTD2DBatch, auto_batch_size, engine_tuning
 
 __all__ = ["TorchLeastSquaresFWI", "forward_store", "forward_store_batch", "stored_steps",
@@ -157,6 +158,7 @@ class TorchLeastSquaresFWI:
         self.source_history = []
         self.mask = np.asarray(mask, dtype=bool)
         self._mask_dev = torch.as_tensor(self.mask, device=dev)
+        self._mask_u8 = self._mask_dev.to(torch.uint8).contiguous()
         self.alpha = float(alpha)
         self.tv = float(tv)
         self.tv_eps = float(tv_eps)
@@ -183,6 +185,10 @@ class TorchLeastSquaresFWI:
         residual = (predicted - observed).clone()
         residual[tx].zero_()
         return residual
+
+    def _mute(self, shot_batch):
+        """Receiver channel zeroed per shot: the transmitter's own (invert_ring.py:603-609)."""
+        return np.asarray(shot_batch)
 
     def _sample_sources(self):
         if self.n_shots == self.array.n_elements:
@@ -236,32 +242,41 @@ class TorchLeastSquaresFWI:
             plan = self._plan(shot_batch, for_gradient=False)
             predicted = plan.forward()
             observed = self.observed[torch.as_tensor(shot_batch, device=self.model.device)]
-            residual_misfit(predicted, observed, np.asarray(shot_batch), residual=predicted, misfit=total)
+            residual_misfit(predicted, observed, self._mute(shot_batch), residual=predicted, misfit=total)
         regularization, _ = self.regularization(m)
         return float(total.item()) + regularization
 
     def misfit_and_grad(self, m):
         """J(m) and g_m = dJ/dm (float64, zero outside the mask) (invert_ring.py:634-660)."""
-        m = self.apply_medium(m)
-        sources = self._sample_sources()
-        self.solver._sync_medium()
+        value, gradient = self.misfit_and_grad_device(torch.as_tensor(np.asarray(m, dtype=float)))
+        return value, gradient.cpu().numpy()
+
+    def misfit_and_grad_device(self, m):
+        """``misfit_and_grad`` with m, the gradient and the regularisers on the device.
+
+        ``m``: float64 (ny, nx) tensor (moved to the device if needed; not modified).
+        Returns the float objective and g_m as a float64 device tensor, zero outside
+        the mask. Only the objective is read back to the host.
+        """
         dev = self.model.device
         medium = self.solver.medium
+        m = torch.as_tensor(m, dtype=torch.float64).to(dev).contiguous().clone()
+        project_device(m, self._mask_u8, self.c_min, self.c_max, self.c_background)
+        self.solver.set_c(1.0 / torch.sqrt(m))
+        sources = self._sample_sources()
+        self.solver._sync_medium()
         total = torch.zeros(1, dtype=torch.float64, device=dev)
         g_c2 = torch.zeros((medium.ny, medium.pitch), dtype=torch.float64, device=dev)
         for shot_batch in self._source_batches(sources):
             plan = self._plan(shot_batch, for_gradient=True)
             predicted = plan.forward(save_checkpoints=True)
             observed = self.observed[torch.as_tensor(shot_batch, device=dev)]
-            residual, _ = residual_misfit(predicted, observed, np.asarray(shot_batch), residual=predicted,
+            residual, _ = residual_misfit(predicted, observed, self._mute(shot_batch), residual=predicted,
                                           misfit=total)
             plan.adjoint(residual, g_c2)
-        m_dev = torch.as_tensor(m, device=dev, dtype=torch.float64)
-        g_m = chain_rule(g_c2[:, :medium.nx].contiguous(), m_dev, self._mask_dev)
-        regularization, g_reg = self.regularization(m)
-        gradient = g_m.cpu().numpy() + g_reg
-        gradient[~self.mask] = 0.0
-        return float(total.item()) + regularization, gradient
+        g_m = chain_rule(g_c2[:, :medium.nx].contiguous(), m, self._mask_dev)
+        regularization_device(m, self._mask_u8, self.alpha, self.tv, self.tv_eps, g_m, total)
+        return float(total.item()), g_m
 
     def gradient_c2(self, m, sources):
         """Unmasked g_{c^2} and the data misfit for fixed transmitters (no projection, no sampling)."""
@@ -276,10 +291,23 @@ class TorchLeastSquaresFWI:
             plan = self._plan(shot_batch, for_gradient=True)
             predicted = plan.forward(save_checkpoints=True)
             observed = self.observed[torch.as_tensor(shot_batch, device=dev)]
-            residual, _ = residual_misfit(predicted, observed, np.asarray(shot_batch), residual=predicted,
+            residual, _ = residual_misfit(predicted, observed, self._mute(shot_batch), residual=predicted,
                                           misfit=total)
             plan.adjoint(residual, g_c2)
         return float(total.item()), g_c2[:, :medium.nx].cpu().numpy()
+
+
+class ArcLeastSquaresFWI(TorchLeastSquaresFWI):
+    """FWI with separate transmit (``array``) and receive (``sampler``) arcs
+    (invert_arc.py:294-307): no transmitter is also a receiver, so the full
+    residual is kept (no muting)."""
+
+    @staticmethod
+    def _residual(predicted, observed, tx):
+        return predicted - observed
+
+    def _mute(self, shot_batch):
+        return None
 
 
 class WaveformMisfit(torch.autograd.Function):

@@ -139,7 +139,22 @@ class TorchScalarWave2D:
         return self._c2
 
     def set_c(self, c):
-        """Update the sound speed in place (fdtd2d/torch_backend.py:158-168)."""
+        """Update the sound speed in place (fdtd2d/torch_backend.py:158-168).
+
+        A tensor already on this CUDA device is taken without a host round trip.
+        """
+        if isinstance(c, torch.Tensor) and c.device == self.device:
+            c64 = c.detach().to(torch.float64)
+            if tuple(c64.shape) != self.shape:
+                raise ValueError(f"Sound speed shape {tuple(c64.shape)} does not match {self.shape}.")
+            if not bool(torch.isfinite(c64).all()) or not bool((c64 > 0).all()):
+                raise ValueError("Sound speed must contain finite positive values.")
+            self._c64.copy_(c64)
+            self._c.copy_(c64)
+            self._c2.copy_(self._c.square())
+            self._c_max = float(c64.max())
+            self.version += 1
+            return
         src = c.detach().cpu().numpy() if isinstance(c, torch.Tensor) else c
         c64 = torch.tensor(np.asarray(src, dtype=np.float64))
         if tuple(c64.shape) != self.shape:
@@ -417,6 +432,49 @@ def simulate_shot(solver: TorchFDTD2D, sampler: TorchRingSampler, pulse, source_
     r = solver._rot
     traces = plan.forward(u_prev_out=r.buf[r.io], u_out=r.buf[r.ic])
     return traces[0], []
+
+
+def simulate_sources(solver: TorchFDTD2D, sampler: TorchRingSampler, source_rows, source_cols, source_values,
+                     n_steps: int, snapshot_steps=()):
+    """Every transmit element fires at once with its own waveform; the receivers record.
+
+    The multi-element firing of 2DArcFDTD.py:203-228 (``simulate``) through the
+    fused engine: ``source_values`` is ``(K, n_steps)``, one waveform per element
+    at ``(source_rows[k], source_cols[k])``; elements that round to one grid node
+    add up, like the reference's ``index_put_(..., accumulate=True)``. Returns
+    traces ``(R, n_steps)`` on the device and a dict of host snapshots for
+    ``snapshot_steps`` (those runs take the per-step form, as the reference does).
+    """
+    rows = np.asarray(source_rows, dtype=np.int64).reshape(-1)
+    cols = np.asarray(source_cols, dtype=np.int64).reshape(-1)
+    if rows.shape != cols.shape:
+        raise ValueError("source_rows and source_cols must have the same length.")
+    dev = solver.model.device
+    values = torch.as_tensor(source_values, device=dev, dtype=torch.float32)
+    if values.ndim != 2 or tuple(values.shape) != (rows.size, int(n_steps)):
+        raise ValueError("source_values must be (n_sources, n_steps).")
+    solver.reset()
+    solver._sync_medium()
+    snapshot_steps = set(int(s) for s in snapshot_steps)
+    if snapshot_steps:
+        rows_t = torch.as_tensor(rows, device=dev)
+        cols_t = torch.as_tensor(cols, device=dev)
+        source_field = torch.zeros(solver.model.shape, device=dev, dtype=torch.float32)
+        traces = torch.empty((sampler.n_elements, int(n_steps)), device=dev, dtype=torch.float32)
+        snapshots = {}
+        for step in range(int(n_steps)):
+            source_field.zero_()
+            source_field.index_put_((rows_t, cols_t), values[:, step].contiguous(), accumulate=True)
+            field = solver.inject_field_and_step(source_field, adjoint=False)
+            traces[:, step] = sampler.record(field)
+            if step in snapshot_steps:
+                snapshots[step] = field.detach().cpu().numpy().copy()
+        return traces, snapshots
+    plan = _plan_for(solver, solver, sampler, rows[None], cols[None], int(n_steps), values.contiguous(),
+                     waves=np.arange(rows.size, dtype=np.int64)[None])
+    r = solver._rot
+    traces = plan.forward(u_prev_out=r.buf[r.io], u_out=r.buf[r.ic])
+    return traces[0], {}
 
 
 class TorchFDTD2DBatch:

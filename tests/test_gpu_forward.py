@@ -234,3 +234,30 @@ def test_fused_many_sources_per_shot(tb, tuning):
         tr, _, _, _ = orc.simulate_shots_batch(p["c"], p["dx"], p["dy"], p["dt"], geo, fields, values, nt)
         ref += tr
     assert rel(traces, ref) < TRACE_TOL
+
+
+def test_simulate_sources_arc_firing_matches_per_step_form(tb):
+    """Focused firing of a 16-element transmit arc, each element with its own
+    delayed chirp, recorded on a separate receive arc: the fused engine against
+    the per-step dense-injection form (2DArcFDTD.py:203-228)."""
+    from soundwavesimulation_gb300 import ArcArray, axis_centers, linear_chirp, stable_dt
+    n, dx, nt = 96, 0.4e-3, 160
+    x = axis_centers(n, dx)
+    c = np.full((n, n), 1500.0)
+    c[30:60, 40:70] = 1650.0
+    dt = stable_dt(1650.0, dx, dx, cfl=0.4)
+    tx = ArcArray(16, 0.4 * n * dx, 60.0, 180.0, x, x)
+    rx = ArcArray(20, 0.4 * n * dx, 60.0, 0.0, x, x)
+    model = tb.TorchScalarWave2D(c, dx, device="cuda")
+    solver = tb.TorchFDTD2D(model, dt)
+    sampler = tb.TorchRingSampler(rx, device="cuda")
+    pulse = linear_chirp(dt, 60 * dt, 2e5, 6e5)
+    values = np.zeros((tx.n_elements, nt))
+    for k in range(tx.n_elements):
+        d = 2 * k
+        values[k, d:d + pulse.size] = pulse[:nt - d]
+    fused, _ = tb.simulate_sources(solver, sampler, tx.rows, tx.cols, values, nt)
+    fused = fused.cpu().numpy()
+    stepped, snaps = tb.simulate_sources(solver, sampler, tx.rows, tx.cols, values, nt, snapshot_steps=(nt - 1,))
+    assert rel(fused, stepped.cpu().numpy()) < 1e-6
+    assert set(snaps) == {nt - 1}
