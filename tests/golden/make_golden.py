@@ -252,6 +252,68 @@ def main() -> None:
     geo.update(geo_arrays(arc, prefix="arc41_"))
     geo["arc41_meta"] = np.array([41, SP, 16, 0.030, 120.0, 90.0])
     np.savez_compressed(OUT / "geometry.npz", **geo)
+
+    # --- F: separate transmit / receive arcs (invert_arc.py, 2DArcFDTD.py) and the
+    # trace file of 2DRingFDTD.py. The drivers are scripts; they load by path.
+    import importlib.util
+
+    def load_script(name, file):
+        spec = importlib.util.spec_from_file_location(name, REFERENCE / file)
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        return mod
+
+    sys.path.insert(0, str(REFERENCE))
+    arc_fwi = load_script("ref_invert_arc", "invert_arc.py")
+    arc_cli = load_script("ref_arc_cli", "2DArcFDTD.py")
+    ring_cli = load_script("ref_ring_cli", "2DRingFDTD.py")
+    # F1: the arc gradient problem of run_arc_gradient_check (invert_arc.py:340-372), float64
+    src_v = torch.zeros(n_steps, dtype=f64)
+    src_v[:pulse.numel()].copy_(pulse)
+    solver_f = TorchFDTD2D(TorchScalarWave2D(c_true.copy(), SP, device="cpu", dtype=f64), dt)
+    tx_arc = ArcArray(3, RAD, 60.0, arc_fwi.TX_CENTER_DEG, x_m, x_m)
+    rx_arc = ArcArray(5, RAD, 60.0, arc_fwi.RX_CENTER_DEG, x_m, x_m)
+    sampler_f = TorchRingSampler(rx_arc, device="cpu", dtype=f64)
+    observed_f = arc_fwi.simulate_observed(solver_f, sampler_f, tx_arc, pulse, src_v, n_steps,
+                                           parallel_shots=3, batched_solvers={})
+    mask_f = interior_mask(x_m, x_m, RAD, margin_m=2.0 * SP)
+    problem_f = arc_fwi.ArcLeastSquaresFWI(solver_f, sampler_f, tx_arc, pulse, n_steps, 3, observed_f, mask_f,
+                                           c_min=1400.0, c_max=2000.0, c_background=1500.0, shot_seed=0)
+    rng_f = np.random.default_rng(0)
+    m0_f = np.full((N, N), 1.0 / 1500.0 ** 2)
+    m0_f[mask_f] *= 1.0 + 0.02 * rng_f.standard_normal(int(mask_f.sum()))
+    m0_f = problem_f.project(m0_f)
+    value_f, grad_f = problem_f.misfit_and_grad(m0_f.copy())
+    # F2: focused firing of an 8-element transmit arc recorded on a 6-element receive arc
+    n2, sp2, rad2, nt2 = 64, 1.0e-3, 0.025, 200
+    x2 = axis_centers(n2, sp2)
+    c2 = np.full((n2, n2), 1500.0)
+    c2[np.add.outer(x2 ** 2, x2 ** 2) <= 0.008 ** 2] = 1650.0
+    dt2 = stable_dt(1650.0, sp2, sp2, cfl=0.45)
+    tx2 = ArcArray(8, rad2, 60.0, arc_cli.TX_CENTER_DEG, x2, x2)
+    rx2 = ArcArray(6, rad2, 60.0, arc_cli.RX_CENTER_DEG, x2, x2)
+    delays2, _ = arc_cli.focusing_delays(tx2, (0.0, 0.0), 1500.0)
+    values2 = arc_cli.delayed_chirps(nt2, dt2, delays2, 40)
+    solver2 = TorchFDTD2D(TorchScalarWave2D(c2.copy(), sp2, device="cpu", dtype=f64), dt2)
+    sampler2 = TorchRingSampler(rx2, device="cpu", dtype=f64)
+    traces2, _ = arc_cli.simulate(solver2, sampler2, tx2, values2, nt2, set())
+    np.savez_compressed(
+        OUT / "arcs.npz",
+        c=c_true, dx=SP, dt=dt, pulse=pulse.numpy(), n_steps=n_steps, radius=RAD,
+        tx_center=arc_fwi.TX_CENTER_DEG, rx_center=arc_fwi.RX_CENTER_DEG, observed=observed_f.numpy(),
+        mask=mask_f, m0=m0_f, value=value_f, gradient=grad_f,
+        focus_c=c2, focus_dx=sp2, focus_dt=dt2, focus_radius=rad2, focus_nt=nt2,
+        focus_tx_center=arc_cli.TX_CENTER_DEG, focus_rx_center=arc_cli.RX_CENTER_DEG,
+        focus_values=values2, focus_traces=traces2,
+        **geo_arrays(tx_arc, prefix="tx_"), **geo_arrays(rx_arc, prefix="rx_"),
+        **geo_arrays(tx2, prefix="focus_tx_"), **geo_arrays(rx2, prefix="focus_rx_"),
+    )
+    # F3: the trace file written by the forward CLI's save_traces (2DRingFDTD.py:291-327)
+    ring6 = RingArray(6, RAD, x_m, x_m)
+    tr_small = np.random.default_rng(3).standard_normal((6, 9)).astype(np.float32)
+    ring_cli.save_traces(OUT / "trace_file.npz", tr_small, np.arange(9) * dt, ring6, 2,
+                         np.linspace(0.0, 1.0, 5), dt, c_map=c_true[:4, :4], device="cuda:0",
+                         dtype="float32", compiled=True, transmitter_indices=[2, 4])
     for p in sorted(OUT.glob("*.npz")):
         print(f"{p.name}: {p.stat().st_size / 1024:.1f} KB")
 

@@ -140,3 +140,42 @@ def test_arc_geometry(golden):
         np.testing.assert_array_equal(g[key], d[f"arc41_{key}"])
     for key in ("w00", "w10", "w01", "w11"):
         np.testing.assert_allclose(g[key], d[f"arc41_{key}"], rtol=0, atol=1e-14)
+
+
+def _arc_pair(d, prefix, n_tx, n_rx, n, dx):
+    ax = orc.axis_centers(n, dx)
+    radius = float(d[f"{prefix}radius"])
+    tx = orc.arc_geometry(n_tx, radius, 60.0, float(d[f"{prefix}tx_center"]), ax, ax)
+    rx = orc.arc_geometry(n_rx, radius, 60.0, float(d[f"{prefix}rx_center"]), ax, ax)
+    for key in ("rows", "cols", "row0", "col0"):
+        np.testing.assert_array_equal(tx[key], d[f"{prefix}tx_{key}"])
+        np.testing.assert_array_equal(rx[key], d[f"{prefix}rx_{key}"])
+    return tx, rx
+
+
+def test_arc_focused_firing(golden):
+    """2DArcFDTD.py:203-228: eight transmit elements fire at once, each with its own
+    delayed chirp; the oracle superposes one run per element (linearity)."""
+    d = golden("arcs")
+    n, dx, nt = d["focus_c"].shape[0], float(d["focus_dx"]), int(d["focus_nt"])
+    tx, rx = _arc_pair(d, "focus_", 8, 6, n, dx)
+    fields = orc.point_sources((n, n), tx["rows"], tx["cols"])
+    traces, _, _, _ = orc.simulate_shots_batch(d["focus_c"], dx, dx, float(d["focus_dt"]), rx, fields,
+                                               d["focus_values"], nt)
+    assert rel(traces.sum(0), d["focus_traces"]) < 1e-10
+
+
+def test_arc_gradient_without_muting(golden):
+    """ArcLeastSquaresFWI.misfit_and_grad (invert_arc.py:294-307): three transmit
+    elements, five receivers on a separate arc, the full residual kept."""
+    d = golden("arcs")
+    n, dx, nt = d["c"].shape[0], float(d["dx"]), int(d["n_steps"])
+    tx, rx = _arc_pair(d, "", 3, 5, n, dx)
+    values = np.zeros(nt)
+    values[:d["pulse"].size] = d["pulse"]
+    src = orc.point_sources((n, n), tx["rows"], tx["cols"])
+    m0 = d["m0"]
+    J, g_c2 = orc.misfit_and_gradient_c2(1.0 / np.sqrt(m0), dx, dx, float(d["dt"]), rx, src, values, nt,
+                                         d["observed"], np.full(3, -1))
+    assert J == pytest.approx(float(d["value"]), rel=1e-10)
+    assert rel(orc.gradient_m(g_c2, m0, d["mask"]), d["gradient"]) < 1e-9
