@@ -294,6 +294,14 @@ int32_t fdtd_project(int64_t n, double* m, const uint8_t* mask, double m_min, do
 int32_t fdtd_adam_step(int64_t n, double* m, const double* grad, const uint8_t* mask, double* first,
                        double* second, double learning_rate, double beta1, double beta2, double epsilon,
                        int32_t iteration, double m_min, double m_max, double m_exterior, void* stream);
+/* Bicubic transfer of m (float64, device) between grid levels in physical
+   coordinates: src_x / src_y and dst_x / dst_y are the device cell-centre axes;
+   target points outside the source grid get `background`. Replaces
+   resize_slowness (invert_ring.py:1048-1068), which calls torch grid_sample
+   (bicubic, border padding, align_corners). */
+int32_t fdtd_resize_slowness(const double* src, int32_t src_ny, int32_t src_nx, const double* src_x,
+                             const double* src_y, double* dst, int32_t dst_ny, int32_t dst_nx,
+                             const double* dst_x, const double* dst_y, double background, void* stream);
 
 #ifdef __cplusplus
 }

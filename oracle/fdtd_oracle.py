@@ -374,3 +374,49 @@ def interior_mask(x_m, y_m, radius_m, margin_m, center=(0.0, 0.0)):
     x, y = np.meshgrid(x_m, y_m, indexing="xy")
     r = float(radius_m) - float(margin_m)
     return (x - center[0]) ** 2 + (y - center[1]) ** 2 < r * r
+
+
+def resize_slowness(m, source_axes, target_axes, background_m):
+    """Bicubic transfer of m between grid levels (invert_ring.py:1048-1068).
+
+    The reference calls ``torch.nn.functional.grid_sample`` (PyTorch, bicubic,
+    ``padding_mode="border"``, ``align_corners=True``) in float64. Restated here
+    from that operator's published definition: Keys' cubic convolution with
+    a = -0.75 on the 4 x 4 neighbours, along x first, then y, neighbour indices
+    clamped into the grid; points outside the source grid get ``background_m``.
+    """
+    m = np.asarray(m, dtype=float)
+    sx, sy = (np.asarray(a, dtype=float) for a in source_axes)
+    tx, ty = (np.asarray(a, dtype=float) for a in target_axes)
+    u = 2.0 * (tx - sx[0]) / (sx[-1] - sx[0]) - 1.0
+    v = 2.0 * (ty - sy[0]) / (sy[-1] - sy[0]) - 1.0
+    vv, uu = np.meshgrid(v, u, indexing="ij")
+    ny, nx = m.shape
+    fx = ((uu + 1.0) / 2.0) * (nx - 1)
+    fy = ((vv + 1.0) / 2.0) * (ny - 1)
+    x0, y0 = np.floor(fx), np.floor(fy)
+    tx_, ty_ = fx - x0, fy - y0
+    a = -0.75
+
+    def near(x):
+        return ((a + 2.0) * x - (a + 3.0)) * x * x + 1.0
+
+    def far(x):
+        return ((a * x - 5.0 * a) * x + 8.0 * a) * x - 4.0 * a
+
+    def weights(t):
+        s = 1.0 - t
+        return far(t + 1.0), near(t), near(s), far(s + 1.0)
+
+    ix, iy = x0.astype(np.int64), y0.astype(np.int64)
+    wx, wy = weights(tx_), weights(ty_)
+    out = np.zeros(uu.shape)
+    for r in range(4):
+        yy = np.clip(iy - 1 + r, 0, ny - 1)
+        row = np.zeros(uu.shape)
+        for q in range(4):
+            xx = np.clip(ix - 1 + q, 0, nx - 1)
+            row = row + m[yy, xx] * wx[q]
+        out = out + row * wy[r]
+    out[(np.abs(uu) > 1.0) | (np.abs(vv) > 1.0)] = background_m
+    return out

@@ -72,6 +72,8 @@ _SIGNATURES = {
     "fdtd_regularization": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_double, c_double, c_double,
                                       c_void_p, c_void_p, c_void_p]),
     "fdtd_project": (c_int32, [ctypes.c_int64, c_void_p, c_void_p, c_double, c_double, c_double, c_void_p]),
+    "fdtd_resize_slowness": (c_int32, [c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
+                                       c_void_p, c_void_p, c_double, c_void_p]),
     "fdtd_adam_step": (c_int32, [ctypes.c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_double,
                                  c_double, c_double, c_double, c_int32, c_double, c_double, c_double,
                                  c_void_p]),

@@ -127,6 +127,68 @@ __global__ void adam_kernel(long long n, double* m, const double* __restrict__ g
   m[i] = project1(v, inside, lo, hi, ext);
 }
 
+// ---- bicubic transfer of m between grid levels (invert_ring.py:1048-1068)
+//
+// The reference calls torch.nn.functional.grid_sample(mode="bicubic",
+// padding_mode="border", align_corners=True) in float64. Its bicubic is Keys'
+// cubic convolution with a = -0.75 on the 4 x 4 neighbours of the source
+// position, rows interpolated first along x, then the four results along y;
+// each neighbour index is clamped into the grid (border padding).
+
+constexpr double CUBIC_A = -0.75;
+
+__device__ __forceinline__ double cubic_near(double x) {  // |x| <= 1
+  return __dadd_rn(__dmul_rn(__dmul_rn(__dsub_rn(__dmul_rn(CUBIC_A + 2.0, x), CUBIC_A + 3.0), x), x), 1.0);
+}
+
+__device__ __forceinline__ double cubic_far(double x) {  // 1 < |x| < 2
+  return __dsub_rn(
+      __dmul_rn(__dadd_rn(__dmul_rn(__dsub_rn(__dmul_rn(CUBIC_A, x), 5.0 * CUBIC_A), x), 8.0 * CUBIC_A), x),
+      4.0 * CUBIC_A);
+}
+
+__device__ __forceinline__ double cubic_1d(double v0, double v1, double v2, double v3, double t) {
+  const double c0 = cubic_far(__dadd_rn(t, 1.0)), c1 = cubic_near(t);
+  const double s = __dsub_rn(1.0, t);
+  const double c2 = cubic_near(s), c3 = cubic_far(__dadd_rn(s, 1.0));
+  return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v0, c0), __dmul_rn(v1, c1)), __dmul_rn(v2, c2)), __dmul_rn(v3, c3));
+}
+
+__device__ __forceinline__ double tap(const double* src, int ny, int nx, long long iy, long long ix) {
+  const long long y = iy < 0 ? 0 : (iy > ny - 1 ? ny - 1 : iy);
+  const long long x = ix < 0 ? 0 : (ix > nx - 1 ? nx - 1 : ix);
+  return src[y * nx + x];
+}
+
+__global__ void resize_kernel(const double* __restrict__ src, int sny, int snx, const double* __restrict__ sx,
+                              const double* __restrict__ sy, double* __restrict__ dst, int tny, int tnx,
+                              const double* __restrict__ tx, const double* __restrict__ ty, double background) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)tny * tnx) return;
+  const int i = (int)(idx / tnx), j = (int)(idx - (long long)i * tnx);
+  // normalised coordinates as the reference builds them on the host
+  const double u = __dsub_rn(__ddiv_rn(__dmul_rn(2.0, __dsub_rn(tx[j], sx[0])), __dsub_rn(sx[snx - 1], sx[0])), 1.0);
+  const double v = __dsub_rn(__ddiv_rn(__dmul_rn(2.0, __dsub_rn(ty[i], sy[0])), __dsub_rn(sy[sny - 1], sy[0])), 1.0);
+  if (fabs(u) > 1.0 || fabs(v) > 1.0) {
+    dst[idx] = background;
+    return;
+  }
+  // align_corners = True: ((coord + 1) / 2) * (size - 1)
+  const double fx = __dmul_rn(__ddiv_rn(__dadd_rn(u, 1.0), 2.0), (double)(snx - 1));
+  const double fy = __dmul_rn(__ddiv_rn(__dadd_rn(v, 1.0), 2.0), (double)(sny - 1));
+  const double x0 = floor(fx), y0 = floor(fy);
+  const double tx_ = __dsub_rn(fx, x0), ty_ = __dsub_rn(fy, y0);
+  const long long ix = (long long)x0, iy = (long long)y0;
+  double rows[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const long long yy = iy - 1 + r;
+    rows[r] = cubic_1d(tap(src, sny, snx, yy, ix - 1), tap(src, sny, snx, yy, ix), tap(src, sny, snx, yy, ix + 1),
+                       tap(src, sny, snx, yy, ix + 2), tx_);
+  }
+  dst[idx] = cubic_1d(rows[0], rows[1], rows[2], rows[3], ty_);
+}
+
 int blocks(long long n) { return (int)((n + BLOCK - 1) / BLOCK); }
 
 }  // namespace
@@ -171,4 +233,17 @@ extern "C" int32_t fdtd_adam_step(int64_t n, double* m, const double* grad, cons
                                                              m_exterior);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "adam launch");
+}
+
+extern "C" int32_t fdtd_resize_slowness(const double* src, int32_t src_ny, int32_t src_nx, const double* src_x,
+                                        const double* src_y, double* dst, int32_t dst_ny, int32_t dst_nx,
+                                        const double* dst_x, const double* dst_y, double background,
+                                        void* stream) {
+  if (!src || !dst || !src_x || !src_y || !dst_x || !dst_y) return fail(FDTD_ERR_INVALID, "resize: null argument");
+  if (src_ny < 2 || src_nx < 2 || dst_ny < 1 || dst_nx < 1) return fail(FDTD_ERR_INVALID, "resize: grids too small");
+  const long long n = (long long)dst_ny * dst_nx;
+  resize_kernel<<<blocks(n), BLOCK, 0, (cudaStream_t)stream>>>(src, src_ny, src_nx, src_x, src_y, dst, dst_ny,
+                                                               dst_nx, dst_x, dst_y, background);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "resize launch");
 }

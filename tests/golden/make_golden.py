@@ -314,6 +314,19 @@ def main() -> None:
     ring_cli.save_traces(OUT / "trace_file.npz", tr_small, np.arange(9) * dt, ring6, 2,
                          np.linspace(0.0, 1.0, 5), dt, c_map=c_true[:4, :4], device="cuda:0",
                          dtype="float32", compiled=True, transmitter_indices=[2, 4])
+    # --- G: multiscale stage transfer (invert_ring.py:1037-1068)
+    from invert_ring import multiscale_stages, resize_slowness
+    rng_g = np.random.default_rng(11)
+    sx = axis_centers(41, 2.0e-3)
+    tx_g = axis_centers(64, 1.4e-3) + 3.0e-3   # finer grid, shifted field of view
+    ty_g = axis_centers(57, 1.6e-3) - 5.0e-3
+    xx_g, yy_g = np.meshgrid(sx, sx, indexing="xy")
+    m_g = 1.0 / (1500.0 + 80.0 * np.sin(90.0 * xx_g) * np.cos(70.0 * yy_g) + rng_g.normal(0, 2.0, xx_g.shape)) ** 2
+    resized = resize_slowness(m_g, (sx, sx), (tx_g, ty_g), 1.0 / 1500.0 ** 2)
+    np.savez_compressed(
+        OUT / "multiscale.npz", m=m_g, sx=sx, sy=sx, tx=tx_g, ty=ty_g, background=1.0 / 1500.0 ** 2,
+        resized=resized, stages_on=np.array(multiscale_stages(True)), stages_off=np.array(multiscale_stages(False)),
+    )
     for p in sorted(OUT.glob("*.npz")):
         print(f"{p.name}: {p.stat().st_size / 1024:.1f} KB")
 

@@ -74,3 +74,14 @@ def test_focused_arc_firing_matches_reference(mods, golden):
     solver, sampler, tx, _ = _arc_setup(tb, d, "focus_", 8, 6, "focus_c", "focus_dx", "focus_dt")
     out, _ = tb.simulate_sources(solver, sampler, tx.rows, tx.cols, d["focus_values"], int(d["focus_nt"]))
     assert rel(out.cpu().numpy(), d["focus_traces"]) < 1e-5
+
+
+def test_resize_slowness_matches_reference(mods, golden):
+    """Stage transfer of the multiscale driver (invert_ring.py:1048-1068) on the GPU."""
+    from soundwavesimulation_gb300.multiscale import resize_slowness
+    d = golden("multiscale")
+    out = resize_slowness(d["m"], (d["sx"], d["sy"]), (d["tx"], d["ty"]), float(d["background"]))
+    np.testing.assert_allclose(out, d["resized"], rtol=1e-13, atol=0.0)
+    dev = resize_slowness(torch.as_tensor(d["m"], device="cuda"), (d["sx"], d["sy"]), (d["tx"], d["ty"]),
+                          float(d["background"]))
+    assert dev.is_cuda and np.array_equal(dev.cpu().numpy(), out)

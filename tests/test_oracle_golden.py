@@ -179,3 +179,18 @@ def test_arc_gradient_without_muting(golden):
                                          d["observed"], np.full(3, -1))
     assert J == pytest.approx(float(d["value"]), rel=1e-10)
     assert rel(orc.gradient_m(g_c2, m0, d["mask"]), d["gradient"]) < 1e-9
+
+
+def test_resize_slowness(golden):
+    """invert_ring.py:1048-1068 (torch grid_sample, bicubic, border, corners aligned)."""
+    d = golden("multiscale")
+    out = orc.resize_slowness(d["m"], (d["sx"], d["sy"]), (d["tx"], d["ty"]), float(d["background"]))
+    np.testing.assert_allclose(out, d["resized"], rtol=1e-13, atol=0.0)
+    assert (out == float(d["background"])).any() and (out != float(d["background"])).any()
+
+
+def test_multiscale_stage_ladder(golden):
+    from soundwavesimulation_gb300.multiscale import multiscale_stages
+    d = golden("multiscale")
+    np.testing.assert_array_equal(np.array(multiscale_stages(True)), d["stages_on"])
+    np.testing.assert_array_equal(np.array(multiscale_stages(False)), d["stages_off"])
