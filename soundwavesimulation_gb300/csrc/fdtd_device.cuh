@@ -164,7 +164,7 @@ struct TbParams {
 // Dynamic shared-memory carve-up of the temporally blocked kernel; the host
 // sizes the launch with the same function.
 struct TbSmem {
-  size_t coef, lap, g, xch, tap, res, src, mask, base, smask, sbase, total;
+  size_t coef, lap, g, xch, mur, tap, res, src, mask, base, smask, sbase, total;
 };
 
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
@@ -187,6 +187,9 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
   }
   m.g = off; if (mode == MODE_ADJ) off += region;
   m.xch = off; off += size_t(2) * nw * 2 * 32 * 16;
+  // Mur table of an edge tile: k set and ratio set, each 2 region heights +
+  // 2 region widths + 8 corner values
+  m.mur = off; off += tb_align16(size_t(2) * (2 * size_t(nw) * ky + 2 * RX + 8) * sizeof(float));
   // tap stage: per step, the full 4-cell row of every (thread, band row) that holds
   // a receiver tap node (forward: recorded values; adjoint: injections, zero
   // where a row's cell has no tap)

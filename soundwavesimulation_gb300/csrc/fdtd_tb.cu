@@ -44,6 +44,7 @@ struct Ctx {
   float* s_lap;
   float* s_g;
   float4* s_xch;
+  float* s_mur;             // the tile's Mur table (edge tiles)
   float* s_tap;
   float* s_src;
 };
@@ -117,20 +118,20 @@ template <int KY, bool WF>
 __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY][4],
                                          const TbParams& p, const Ctx& x) {
   const int nx = p.nx, ny = p.ny;
-  const float* kl = p.mur;
-  const float* kr = kl + ny;
-  const float* kb = kr + ny;
-  const float* kt = kb + nx;
-  const float* ckx = kt + nx;
-  const float* cky = ckx + 4;
-  // w-form adjoint: the inner values scale by coef_edge / coef_inner (1 otherwise)
-  const float* rlw = p.mur + 2 * ny + 2 * nx + 8;
-  const float* rrw = rlw + ny;
-  const float* rbw = rrw + ny;
-  const float* rtw = rbw + nx;
-  const float* crx = rtw + nx;
-  const float* cry = crx + 4;
-  auto R = [&](const float* arr, int j) { return WF ? __ldg(arr + j) : 1.0f; };
+  // the tile's Mur table in shared memory (filled per item, local indices):
+  // k left / right per region row, bottom / top per region column, corner kx[4],
+  // ky[4]; for the w-form adjoint the same layout again holds the ratios
+  // coef_edge / coef_inner that scale the inner values (1 otherwise)
+  const int ry = x.nw * KY;
+  const float* kL = x.s_mur;
+  const float* kR = kL + ry;
+  const float* kB = kR + ry;
+  const float* kT = kB + RX;
+  const float* kC = kT + RX;
+  const int rofs = 2 * ry + 2 * RX + 8;
+  auto R = [&](const float* k, int j) { return WF ? k[rofs + j] : 1.0f; };
+  const int lr0 = x.w * KY;      // region row of band row 0
+  const int lc0 = 4 * x.lane;    // region column of c = 0
   const int rb = -x.y0;          // band row of global row 0
   const int rt = ny - 1 - x.y0;  // band row of global row ny-1
   const bool has_bot = (x.flags & TF_BOTTOM) && rb >= 0 && rb + 1 < KY;   // warp-uniform
@@ -142,7 +143,8 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           const int xx = x.xb + c;
-          if (xx >= 1 && xx <= nx - 2) P[r][c] = murw(R(rbw, xx), C[r + 1][c], __ldg(kb + xx), P[r + 1][c], C[r][c]);
+          if (xx >= 1 && xx <= nx - 2)
+            P[r][c] = murw(R(kB, lc0 + c), C[r + 1][c], kB[lc0 + c], P[r + 1][c], C[r][c]);
         }
       }
     }
@@ -154,7 +156,8 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           const int xx = x.xb + c;
-          if (xx >= 1 && xx <= nx - 2) P[r][c] = murw(R(rtw, xx), C[r - 1][c], __ldg(kt + xx), P[r - 1][c], C[r][c]);
+          if (xx >= 1 && xx <= nx - 2)
+            P[r][c] = murw(R(kT, lc0 + c), C[r - 1][c], kT[lc0 + c], P[r - 1][c], C[r][c]);
         }
       }
     }
@@ -163,31 +166,33 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
       const int yy = x.y0 + r;
-      if (yy >= 1 && yy <= ny - 2) P[r][0] = murw(R(rlw, yy), C[r][1], __ldg(kl + yy), P[r][1], C[r][0]);
+      if (yy >= 1 && yy <= ny - 2) P[r][0] = murw(R(kL, lr0 + r), C[r][1], kL[lr0 + r], P[r][1], C[r][0]);
     }
   }
   if (x.flags & TF_RIGHT) {
     const int lx1 = nx - 1 - x.rx0;
-    const int L1 = lx1 >> 2, c1 = lx1 & 3;
+    const int L1 = lx1 >> 2, c1 = lx1 & 3;   // tile-uniform
     // Column nx-2 sits in the same lane (c1 >= 1) or in column 3 of the previous
-    // lane (c1 == 0, one shuffle pair per row, executed by the whole warp). The
+    // lane (c1 == 0: one shuffle pair per row, executed by the whole warp). The
     // edge rows are updated first, so the corners below see updated values.
+    if (c1 == 0) {
 #pragma unroll
-    for (int r = 0; r < KY; ++r) {
-      float su = 0.f, sn = 0.f;
-      if (c1 == 0) {
-        su = __shfl_up_sync(FULL, C[r][3], 1);
-        sn = __shfl_up_sync(FULL, P[r][3], 1);
+      for (int r = 0; r < KY; ++r) {
+        const float su = __shfl_up_sync(FULL, C[r][3], 1);
+        const float sn = __shfl_up_sync(FULL, P[r][3], 1);
+        const int yy = x.y0 + r;
+        if (x.lane == L1 && yy >= 1 && yy <= ny - 2)
+          P[r][0] = murw(R(kR, lr0 + r), su, kR[lr0 + r], sn, C[r][0]);
       }
-      const int yy = x.y0 + r;
-      if (x.lane == L1 && yy >= 1 && yy <= ny - 2) {
+    } else if (x.lane == L1) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          if (c == c1) {
-            const float uin = (c == 0) ? su : C[r][c > 0 ? c - 1 : 0];
-            const float nin = (c == 0) ? sn : P[r][c > 0 ? c - 1 : 0];
-            P[r][c] = murw(R(rrw, yy), uin, __ldg(kr + yy), nin, C[r][c]);
-          }
+      for (int r = 0; r < KY; ++r) {
+        const int yy = x.y0 + r;
+        if (yy >= 1 && yy <= ny - 2) {
+          const float k = kR[lr0 + r], rr = R(kR, lr0 + r);
+          if (c1 == 1) P[r][1] = murw(rr, C[r][0], k, P[r][0], C[r][1]);
+          else if (c1 == 2) P[r][2] = murw(rr, C[r][1], k, P[r][1], C[r][2]);
+          else P[r][3] = murw(rr, C[r][2], k, P[r][2], C[r][3]);
         }
       }
     }
@@ -210,8 +215,8 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
               if (c == c1) {
                 const float uin = (c == 0) ? su : C[r][c > 0 ? c - 1 : 0];
                 const float nin = (c == 0) ? sn : P[r][c > 0 ? c - 1 : 0];
-                const float fx = murw(R(crx, ci), uin, __ldg(ckx + ci), nin, C[r][c]);
-                const float fy = murw(R(cry, ci), C[rn][c], __ldg(cky + ci), P[rn][c], C[r][c]);
+                const float fx = murw(R(kC, ci), uin, kC[ci], nin, C[r][c]);
+                const float fy = murw(R(kC, 4 + ci), C[rn][c], kC[4 + ci], P[rn][c], C[r][c]);
                 P[r][c] = corner_avg(fx, fy);
               }
             }
@@ -228,8 +233,8 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
       if (bot || top) {
         const int rn = bot ? (r + 1 < KY ? r + 1 : r) : (r >= 1 ? r - 1 : r);
         const int ci = bot ? 0 : 2;
-        const float fx = murw(R(crx, ci), C[r][1], __ldg(ckx + ci), P[r][1], C[r][0]);
-        const float fy = murw(R(cry, ci), C[rn][0], __ldg(cky + ci), P[rn][0], C[r][0]);
+        const float fx = murw(R(kC, ci), C[r][1], kC[ci], P[r][1], C[r][0]);
+        const float fy = murw(R(kC, 4 + ci), C[rn][0], kC[4 + ci], P[rn][0], C[r][0]);
         P[r][0] = corner_avg(fx, fy);
       }
     }
@@ -463,6 +468,7 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   x.s_lap = reinterpret_cast<float*>(smem + L.lap);
   x.s_g = reinterpret_cast<float*>(smem + L.g);
   x.s_xch = reinterpret_cast<float4*>(smem + L.xch);
+  x.s_mur = reinterpret_cast<float*>(smem + L.mur);
   x.s_tap = reinterpret_cast<float*>(smem + L.tap);
   float* s_res = reinterpret_cast<float*>(smem + L.res);
   unsigned* s_mask = reinterpret_cast<unsigned*>(smem + L.mask);
@@ -512,6 +518,26 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
       }
       if (MODE == MODE_ADJ) {
         reinterpret_cast<float4*>(x.s_g)[(x.w * KY + r) * 32 + x.lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    if (t.flags) {
+      // the tile's Mur table: left / right k per region row, bottom / top per
+      // region column, corner kx / ky; the adjoint also copies the ratio set
+      const int ry = nw * KY, len = 2 * ry + 2 * RX + 8, glen = 2 * p.ny + 2 * p.nx + 8;
+      for (int i = x.tid; i < len * (MODE == MODE_ADJ ? 2 : 1); i += nthr) {
+        const int set = i / len, j = i - set * len;
+        const float* g = p.mur + set * glen;
+        float v = 0.f;
+        if (j < 2 * ry) {
+          const int side = j >= ry, gy = t.ry0 + j - side * ry;
+          if (gy >= 0 && gy < p.ny) v = __ldg(g + side * p.ny + gy);
+        } else if (j < 2 * ry + 2 * RX) {
+          const int side = j >= 2 * ry + RX, gx = t.rx0 + j - 2 * ry - side * RX;
+          if (gx >= 0 && gx < p.nx) v = __ldg(g + 2 * p.ny + side * p.nx + gx);
+        } else {
+          v = __ldg(g + 2 * p.ny + 2 * p.nx + (j - 2 * ry - 2 * RX));
+        }
+        x.s_mur[i] = v;
       }
     }
     s_mask[x.tid] = 0u;
