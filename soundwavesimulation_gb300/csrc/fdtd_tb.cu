@@ -114,6 +114,22 @@ __device__ __forceinline__ void prefetch_lap(const TbParams& p, const Ctx& x, in
 // the recompute stores is exact; in the adjoint their operand coef * l is zero,
 // so whatever they hold never reaches a domain cell, and they are never written
 // back.
+// The Mur values of KY consecutive region rows (16-byte aligned in the table).
+template <int KY>
+__device__ __forceinline__ void load_rows(float (&v)[KY], const float* src) {
+#pragma unroll
+  for (int q = 0; q < KY / 4; ++q) {
+    const float4 t = reinterpret_cast<const float4*>(src)[q];
+    v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+  }
+}
+
+// One Mur edge cell; with the ratio r = 1 (forward) murw reduces to mur exactly.
+template <bool WF>
+__device__ __forceinline__ float mur_edge(float r, float w_in, float k, float wn_in, float w_edge) {
+  return WF ? murw(r, w_in, k, wn_in, w_edge) : mur(w_in, k, wn_in, w_edge);
+}
+
 template <int KY, bool WF>
 __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY][4],
                                          const TbParams& p, const Ctx& x) {
@@ -162,11 +178,15 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
       }
     }
   }
+  // rows 1 .. ny-2 of the band take the left / right Mur update
+  const int rlo = 1 - x.y0, rhi = ny - 2 - x.y0;
   if ((x.flags & TF_LEFT) && x.lane == 0) {
+    float k[KY], rr[KY];
+    load_rows<KY>(k, kL + lr0);
+    if (WF) load_rows<KY>(rr, kL + rofs + lr0);
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
-      const int yy = x.y0 + r;
-      if (yy >= 1 && yy <= ny - 2) P[r][0] = murw(R(kL, lr0 + r), C[r][1], kL[lr0 + r], P[r][1], C[r][0]);
+      if (r >= rlo && r <= rhi) P[r][0] = mur_edge<WF>(WF ? rr[r] : 1.0f, C[r][1], k[r], P[r][1], C[r][0]);
     }
   }
   if (x.flags & TF_RIGHT) {
@@ -180,19 +200,20 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
       for (int r = 0; r < KY; ++r) {
         const float su = __shfl_up_sync(FULL, C[r][3], 1);
         const float sn = __shfl_up_sync(FULL, P[r][3], 1);
-        const int yy = x.y0 + r;
-        if (x.lane == L1 && yy >= 1 && yy <= ny - 2)
-          P[r][0] = murw(R(kR, lr0 + r), su, kR[lr0 + r], sn, C[r][0]);
+        if (x.lane == L1 && r >= rlo && r <= rhi)
+          P[r][0] = mur_edge<WF>(R(kR, lr0 + r), su, kR[lr0 + r], sn, C[r][0]);
       }
     } else if (x.lane == L1) {
+      float k[KY], rr[KY];
+      load_rows<KY>(k, kR + lr0);
+      if (WF) load_rows<KY>(rr, kR + rofs + lr0);
 #pragma unroll
       for (int r = 0; r < KY; ++r) {
-        const int yy = x.y0 + r;
-        if (yy >= 1 && yy <= ny - 2) {
-          const float k = kR[lr0 + r], rr = R(kR, lr0 + r);
-          if (c1 == 1) P[r][1] = murw(rr, C[r][0], k, P[r][0], C[r][1]);
-          else if (c1 == 2) P[r][2] = murw(rr, C[r][1], k, P[r][1], C[r][2]);
-          else P[r][3] = murw(rr, C[r][2], k, P[r][2], C[r][3]);
+        if (r >= rlo && r <= rhi) {
+          const float q = WF ? rr[r] : 1.0f;
+          if (c1 == 1) P[r][1] = mur_edge<WF>(q, C[r][0], k[r], P[r][0], C[r][1]);
+          else if (c1 == 2) P[r][2] = mur_edge<WF>(q, C[r][1], k[r], P[r][1], C[r][2]);
+          else P[r][3] = mur_edge<WF>(q, C[r][2], k[r], P[r][2], C[r][3]);
         }
       }
     }
@@ -259,8 +280,10 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   float4 prv = (x.w > 0) ? xin[(x.w - 1) * 64 + 32 + x.lane] : zero4;
   const float4 below = (x.w < x.nw - 1) ? xin[(x.w + 1) * 64 + x.lane] : zero4;
   float4 cur = opval(C[0]);
-  const bool lzero = EDGE && x.lane == 0 && x.rx0 == 0;
-  const bool rzero = EDGE && x.lane == 31 && (x.rx0 + RX >= p.nx);
+  // Column 0 and column nx-1 are always overwritten by the Mur update, so only
+  // the recompute, which stores lap(u) itself, needs the zero outside the domain.
+  const bool lzero = EDGE && MODE == MODE_REC && x.lane == 0 && x.rx0 == 0;
+  const bool rzero = EDGE && MODE == MODE_REC && x.lane == 31 && (x.rx0 + RX >= p.nx);
   float* segrow = nullptr;
   if (MODE == MODE_REC) {
     segrow = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
