@@ -130,6 +130,25 @@ __device__ __forceinline__ float mur_edge(float r, float w_in, float k, float wn
   return WF ? murw(r, w_in, k, wn_in, w_edge) : mur(w_in, k, wn_in, w_edge);
 }
 
+// Left / right Mur column of one lane: edge column CE, inner column CI of the same
+// lane, band rows rlo..rhi (all rows in the common case, without per-row tests).
+template <int KY, bool WF, int CE, int CI>
+__device__ __forceinline__ void mur_column(float (&P)[KY][4], const float (&C)[KY][4], const float* k,
+                                           const float* ratio, int rlo, int rhi) {
+  float kv[KY], rv[KY];
+  load_rows<KY>(kv, k);
+  if (WF) load_rows<KY>(rv, ratio);
+  if (rlo <= 0 && rhi >= KY - 1) {
+#pragma unroll
+    for (int r = 0; r < KY; ++r)
+      P[r][CE] = mur_edge<WF>(WF ? rv[r] : 1.0f, C[r][CI], kv[r], P[r][CI], C[r][CE]);
+  } else {
+#pragma unroll
+    for (int r = 0; r < KY; ++r)
+      if (r >= rlo && r <= rhi) P[r][CE] = mur_edge<WF>(WF ? rv[r] : 1.0f, C[r][CI], kv[r], P[r][CI], C[r][CE]);
+  }
+}
+
 template <int KY, bool WF>
 __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY][4],
                                          const TbParams& p, const Ctx& x) {
@@ -180,15 +199,7 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
   }
   // rows 1 .. ny-2 of the band take the left / right Mur update
   const int rlo = 1 - x.y0, rhi = ny - 2 - x.y0;
-  if ((x.flags & TF_LEFT) && x.lane == 0) {
-    float k[KY], rr[KY];
-    load_rows<KY>(k, kL + lr0);
-    if (WF) load_rows<KY>(rr, kL + rofs + lr0);
-#pragma unroll
-    for (int r = 0; r < KY; ++r) {
-      if (r >= rlo && r <= rhi) P[r][0] = mur_edge<WF>(WF ? rr[r] : 1.0f, C[r][1], k[r], P[r][1], C[r][0]);
-    }
-  }
+  if ((x.flags & TF_LEFT) && x.lane == 0) mur_column<KY, WF, 0, 1>(P, C, kL + lr0, kL + rofs + lr0, rlo, rhi);
   if (x.flags & TF_RIGHT) {
     const int lx1 = nx - 1 - x.rx0;
     const int L1 = lx1 >> 2, c1 = lx1 & 3;   // tile-uniform
@@ -204,18 +215,9 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
           P[r][0] = mur_edge<WF>(R(kR, lr0 + r), su, kR[lr0 + r], sn, C[r][0]);
       }
     } else if (x.lane == L1) {
-      float k[KY], rr[KY];
-      load_rows<KY>(k, kR + lr0);
-      if (WF) load_rows<KY>(rr, kR + rofs + lr0);
-#pragma unroll
-      for (int r = 0; r < KY; ++r) {
-        if (r >= rlo && r <= rhi) {
-          const float q = WF ? rr[r] : 1.0f;
-          if (c1 == 1) P[r][1] = mur_edge<WF>(q, C[r][0], k[r], P[r][0], C[r][1]);
-          else if (c1 == 2) P[r][2] = mur_edge<WF>(q, C[r][1], k[r], P[r][1], C[r][2]);
-          else P[r][3] = mur_edge<WF>(q, C[r][2], k[r], P[r][2], C[r][3]);
-        }
-      }
+      if (c1 == 3) mur_column<KY, WF, 3, 2>(P, C, kR + lr0, kR + rofs + lr0, rlo, rhi);
+      else if (c1 == 2) mur_column<KY, WF, 2, 1>(P, C, kR + lr0, kR + rofs + lr0, rlo, rhi);
+      else mur_column<KY, WF, 1, 0>(P, C, kR + lr0, kR + rofs + lr0, rlo, rhi);
     }
     if (has_bot || has_top) {  // corners (0, nx-1) and (ny-1, nx-1)
 #pragma unroll
@@ -642,7 +644,14 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
     x.sbase = s_sbase[x.tid];
     // run_item publishes the exchange rows and synchronises before the first step
 
-    if (t.flags) {
+    // Edge code only in warps with edge cells: every warp of a tile holding the
+    // left or right edge (column 0 / nx-1 and the padding columns sit in every
+    // band), only the warps holding row 0 or row ny-1 otherwise. Warps of one CTA
+    // may take different variants: both pass the same per-step barriers.
+    const bool warp_edge = (t.flags & (TF_LEFT | TF_RIGHT)) ||
+                           ((t.flags & TF_BOTTOM) && x.y0 <= 0 && x.y0 + KY > 0) ||
+                           ((t.flags & TF_TOP) && x.y0 <= p.ny - 1 && x.y0 + KY > p.ny - 1);
+    if (warp_edge) {
       run_item<KY, MODE, true>(p, x);
     } else {
       run_item<KY, MODE, false>(p, x);
