@@ -149,6 +149,33 @@ __device__ __forceinline__ void mur_column(float (&P)[KY][4], const float (&C)[K
   }
 }
 
+// Bottom / top Mur row RE of one lane from the inner row RI (columns 1 .. nx-2).
+template <int KY, bool WF, int RE, int RI>
+__device__ __forceinline__ void mur_row(float (&P)[KY][4], const float (&C)[KY][4], const float* k,
+                                        const float* ratio, int xb, int nx) {
+  const float4 kv = *reinterpret_cast<const float4*>(k);
+  const float4 rv = WF ? *reinterpret_cast<const float4*>(ratio) : make_float4(1.f, 1.f, 1.f, 1.f);
+  const float kk[4] = {kv.x, kv.y, kv.z, kv.w}, rr[4] = {rv.x, rv.y, rv.z, rv.w};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float m = mur_edge<WF>(rr[c], C[RI][c], kk[c], P[RI][c], C[RE][c]);
+    if (xb + c >= 1 && xb + c <= nx - 2) P[RE][c] = m;
+  }
+}
+
+// mur_row at the runtime band row `re`, inner row re + DIR (compile-time dispatch).
+template <int KY, bool WF, int DIR, int R = 0>
+__device__ __forceinline__ void mur_row_at(float (&P)[KY][4], const float (&C)[KY][4], int re, const float* k,
+                                           const float* ratio, int xb, int nx) {
+  if constexpr (R + DIR >= 0 && R + DIR < KY) {
+    if (re == R) {
+      mur_row<KY, WF, R, R + DIR>(P, C, k, ratio, xb, nx);
+      return;
+    }
+  }
+  if constexpr (R + 1 < KY) mur_row_at<KY, WF, DIR, R + 1>(P, C, re, k, ratio, xb, nx);
+}
+
 template <int KY, bool WF>
 __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY][4],
                                          const TbParams& p, const Ctx& x) {
@@ -171,32 +198,14 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
   const int rt = ny - 1 - x.y0;  // band row of global row ny-1
   const bool has_bot = (x.flags & TF_BOTTOM) && rb >= 0 && rb + 1 < KY;   // warp-uniform
   const bool has_top = (x.flags & TF_TOP) && rt >= 1 && rt < KY;          // warp-uniform
+  // bottom / top Mur rows on the columns 1 .. nx-2 of this lane (row 0 is band
+  // row 0 of the first warp whenever the region starts at row 0, as the tiler
+  // places it; other positions take the general form)
   if (has_bot) {
-#pragma unroll
-    for (int r = 0; r + 1 < KY; ++r) {
-      if (r == rb) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const int xx = x.xb + c;
-          if (xx >= 1 && xx <= nx - 2)
-            P[r][c] = murw(R(kB, lc0 + c), C[r + 1][c], kB[lc0 + c], P[r + 1][c], C[r][c]);
-        }
-      }
-    }
+    if (rb == 0) mur_row<KY, WF, 0, 1>(P, C, kB + lc0, kB + rofs + lc0, x.xb, nx);
+    else mur_row_at<KY, WF, 1>(P, C, rb, kB + lc0, kB + rofs + lc0, x.xb, nx);
   }
-  if (has_top) {
-#pragma unroll
-    for (int r = 1; r < KY; ++r) {
-      if (r == rt) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const int xx = x.xb + c;
-          if (xx >= 1 && xx <= nx - 2)
-            P[r][c] = murw(R(kT, lc0 + c), C[r - 1][c], kT[lc0 + c], P[r - 1][c], C[r][c]);
-        }
-      }
-    }
-  }
+  if (has_top) mur_row_at<KY, WF, -1>(P, C, rt, kT + lc0, kT + rofs + lc0, x.xb, nx);
   // rows 1 .. ny-2 of the band take the left / right Mur update
   const int rlo = 1 - x.y0, rhi = ny - 2 - x.y0;
   if ((x.flags & TF_LEFT) && x.lane == 0) mur_column<KY, WF, 0, 1>(P, C, kL + lr0, kL + rofs + lr0, rlo, rhi);
