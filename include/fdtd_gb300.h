@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 1
+#define FDTD_ABI_VERSION 2
 
 enum {
   FDTD_OK = 0,
@@ -101,6 +101,9 @@ typedef struct fdtd_tuning {
                                steps_per_launch; 0 = about sqrt(2 nt) */
   int32_t ckpt_store;       /* FDTD_STORE_F32 / _F16 / _BF16 */
   int32_t ctas_per_sm;      /* persistent grid = SMs * ctas_per_sm; 0 = 1 */
+  int32_t eager;            /* 0 (default): fdtd_forward / fdtd_adjoint capture their launch
+                               sequence once per set of output pointers and replay it as a
+                               CUDA graph; 1: launch every kernel from the host */
 } fdtd_tuning;
 
 typedef struct fdtd_plan fdtd_plan; /* opaque host-side execution plan */

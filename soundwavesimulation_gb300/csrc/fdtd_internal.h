@@ -17,6 +17,8 @@ int32_t cuda_fail(cudaError_t e, const char* what);
 
 // Temporally blocked kernel (fdtd_tb.cu).
 cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st);
+// Sets the dynamic shared-memory attribute of the kernel a launch would use.
+cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem);
 
 // One-step kernels and helpers (fdtd_kernels.cu).
 struct StepArgs {

@@ -125,6 +125,25 @@ struct fdtd_plan {
   bool bound = false;
   bool have_ckpt = false;
   int sm_count = 0;
+  // CUDA-graph replay of the launch sequences (captured on a private stream,
+  // launched on the caller's); the key holds every pointer baked into the graph
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    const void* key[4] = {nullptr, nullptr, nullptr, nullptr};
+    int flag = 0;
+  };
+  Graph g_fwd, g_adj;
+  cudaStream_t capture_stream = nullptr;
+  void drop_graphs() {
+    for (Graph* g : {&g_fwd, &g_adj}) {
+      if (g->exec) cudaGraphExecDestroy(g->exec);
+      *g = Graph();
+    }
+  }
+  ~fdtd_plan() {
+    drop_graphs();
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+  }
 };
 
 namespace {
@@ -707,6 +726,7 @@ int32_t fdtd_plan_bind(fdtd_plan* p, void* workspace, size_t bytes, void* stream
   if (e != cudaSuccess) return cuda_fail(e, "table upload sync");
   p->bound = true;
   p->have_ckpt = false;
+  p->drop_graphs();
   return FDTD_OK;
 }
 
@@ -717,16 +737,57 @@ int32_t fdtd_plan_set_medium(fdtd_plan* p, const float* coef, const float* mur,
   if (mur) p->prob.grid.mur = mur;
   if (waveforms) p->prob.src.waveforms = waveforms;
   p->have_ckpt = false;
+  p->drop_graphs();
   return FDTD_OK;
 }
 
-int32_t fdtd_forward(fdtd_plan* p, float* traces, float* u_prev_out, float* u_out,
-                     int32_t save_checkpoints, void* stream) {
-  if (!p || !p->bound) return fail(FDTD_ERR_STATE, "plan is not bound to a workspace");
-  if (!traces) return fail(FDTD_ERR_INVALID, "traces must be set");
-  if ((u_prev_out == nullptr) != (u_out == nullptr)) return fail(FDTD_ERR_INVALID, "give both final-state outputs or neither");
-  if (save_checkpoints && !p->for_gradient) return fail(FDTD_ERR_STATE, "plan was created without gradient storage");
-  cudaStream_t st = (cudaStream_t)stream;
+}  // extern "C"
+
+namespace {
+
+// Runs `enqueue` on `st`, or replays it as a CUDA graph captured once per key.
+template <typename F>
+int32_t run_graphed(fdtd_plan* p, fdtd_plan::Graph& g, const void* const (&key)[4], int flag,
+                    cudaStream_t st, F enqueue) {
+  if (p->tun.eager) return enqueue(st);
+  bool hit = g.exec != nullptr && g.flag == flag;
+  for (int i = 0; i < 4 && hit; ++i) hit = g.key[i] == key[i];
+  if (!hit) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = fdtd_plan::Graph();
+    cudaError_t e = cudaSuccess;
+    if (!p->capture_stream) e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "capture stream");
+    // kernel attributes are set outside the capture
+    for (int m = 0; m < 3; ++m) {
+      e = tb_configure(p->ky, m, p->nw, p->smem[m]);
+      if (e != cudaSuccess) return cuda_fail(e, "kernel attributes");
+    }
+    e = cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+    const int32_t rc = enqueue(p->capture_stream);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(p->capture_stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "end capture");
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      g.exec = nullptr;
+      return cuda_fail(e, "graph instantiate");
+    }
+    for (int i = 0; i < 4; ++i) g.key[i] = key[i];
+    g.flag = flag;
+  }
+  cudaError_t e = cudaGraphLaunch(g.exec, st);
+  return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "graph launch");
+}
+
+int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u_out,
+                        int32_t save_checkpoints, cudaStream_t st) {
   const size_t fb = p->field_elems * sizeof(float);
   cudaError_t e = cudaMemsetAsync(p->ws + p->o_state[0][0], 0, fb, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(p->ws + p->o_state[0][1], 0, fb, st);
@@ -778,15 +839,10 @@ int32_t fdtd_forward(fdtd_plan* p, float* traces, float* u_prev_out, float* u_ou
     in_cur = out_cur;
     in_set = next_set;
   }
-  p->have_ckpt = save_checkpoints != 0;
   return FDTD_OK;
 }
 
-int32_t fdtd_adjoint(fdtd_plan* p, const float* residual, double* grad_c2, void* stream) {
-  if (!p || !p->bound) return fail(FDTD_ERR_STATE, "plan is not bound to a workspace");
-  if (!p->have_ckpt) return fail(FDTD_ERR_STATE, "run fdtd_forward with save_checkpoints first");
-  if (!residual || !grad_c2) return fail(FDTD_ERR_INVALID, "null pointer");
-  cudaStream_t st = (cudaStream_t)stream;
+int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, cudaStream_t st) {
   const size_t fb = p->field_elems * sizeof(float);
   cudaError_t e = cudaMemsetAsync(p->ws + p->o_adj[0][0], 0, fb, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(p->ws + p->o_adj[0][1], 0, fb, st);
@@ -863,6 +919,35 @@ int32_t fdtd_adjoint(fdtd_plan* p, const float* residual, double* grad_c2, void*
     }
   }
   return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fdtd_forward(fdtd_plan* p, float* traces, float* u_prev_out, float* u_out,
+                     int32_t save_checkpoints, void* stream) {
+  if (!p || !p->bound) return fail(FDTD_ERR_STATE, "plan is not bound to a workspace");
+  if (!traces) return fail(FDTD_ERR_INVALID, "traces must be set");
+  if ((u_prev_out == nullptr) != (u_out == nullptr)) return fail(FDTD_ERR_INVALID, "give both final-state outputs or neither");
+  if (save_checkpoints && !p->for_gradient) return fail(FDTD_ERR_STATE, "plan was created without gradient storage");
+  const void* const key[4] = {traces, u_prev_out, u_out, nullptr};
+  const int32_t rc = run_graphed(p, p->g_fwd, key, save_checkpoints != 0, (cudaStream_t)stream,
+                                 [&](cudaStream_t st) {
+                                   return forward_enqueue(p, traces, u_prev_out, u_out, save_checkpoints, st);
+                                 });
+  if (rc) return rc;
+  p->have_ckpt = save_checkpoints != 0;
+  return FDTD_OK;
+}
+
+int32_t fdtd_adjoint(fdtd_plan* p, const float* residual, double* grad_c2, void* stream) {
+  if (!p || !p->bound) return fail(FDTD_ERR_STATE, "plan is not bound to a workspace");
+  if (!p->have_ckpt) return fail(FDTD_ERR_STATE, "run fdtd_forward with save_checkpoints first");
+  if (!residual || !grad_c2) return fail(FDTD_ERR_INVALID, "null pointer");
+  const void* const key[4] = {residual, grad_c2, nullptr, nullptr};
+  return run_graphed(p, p->g_adj, key, 0, (cudaStream_t)stream,
+                     [&](cudaStream_t st) { return adjoint_enqueue(p, residual, grad_c2, st); });
 }
 
 // ----------------------------------------------------------- plain engine

@@ -404,13 +404,13 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
 #pragma unroll
       for (int r = 0; r < KY; ++r) {
         if ((x.own_rows >> r) & 1u) {
+          // all four columns in pairs: a column this thread does not own sums
+          // whatever its Laplacian slot holds, and is never flushed
           const float4 lv = l4[r * 32];
-          float4 gv = g4[r * 32];
-          if (x.own_cols & 1u) gv.x = __fmaf_rn(P[r][0], lv.x, gv.x);
-          if (x.own_cols & 2u) gv.y = __fmaf_rn(P[r][1], lv.y, gv.y);
-          if (x.own_cols & 4u) gv.z = __fmaf_rn(P[r][2], lv.z, gv.z);
-          if (x.own_cols & 8u) gv.w = __fmaf_rn(P[r][3], lv.w, gv.w);
-          g4[r * 32] = gv;
+          const float4 gv = g4[r * 32];
+          const float2 ga = __ffma2_rn(make_float2(P[r][0], P[r][1]), make_float2(lv.x, lv.y), make_float2(gv.x, gv.y));
+          const float2 gb = __ffma2_rn(make_float2(P[r][2], P[r][3]), make_float2(lv.z, lv.w), make_float2(gv.z, gv.w));
+          g4[r * 32] = make_float4(ga.x, ga.y, gb.x, gb.y);
         }
       }
     }
@@ -701,14 +701,21 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
 }
 
 template <int KY, int MODE, int MAXT>
-cudaError_t launch_one(const TbParams& p, int grid, size_t smem, cudaStream_t st) {
-  static size_t configured_smem = 0;
+cudaError_t configure_one(size_t smem) {
+  static size_t configured_smem = 0;  // per device it is the same binary; raise only
   if (smem > configured_smem) {
     cudaError_t e = cudaFuncSetAttribute(tb_kernel<KY, MODE, MAXT>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured_smem = smem;
   }
+  return cudaSuccess;
+}
+
+template <int KY, int MODE, int MAXT>
+cudaError_t launch_one(const TbParams& p, int grid, size_t smem, cudaStream_t st) {
+  cudaError_t e = configure_one<KY, MODE, MAXT>(smem);
+  if (e != cudaSuccess) return e;
   tb_kernel<KY, MODE, MAXT><<<grid, p.nwarps * 32, smem, st>>>(p);
   return cudaGetLastError();
 }
@@ -718,6 +725,13 @@ cudaError_t launch_mode(const TbParams& p, int mode, int grid, size_t smem, cuda
   if (mode == MODE_FWD) return launch_one<KY, MODE_FWD, MAXT>(p, grid, smem, st);
   if (mode == MODE_REC) return launch_one<KY, MODE_REC, MAXT>(p, grid, smem, st);
   return launch_one<KY, MODE_ADJ, MAXT>(p, grid, smem, st);
+}
+
+template <int KY, int MAXT>
+cudaError_t configure_mode(int mode, size_t smem) {
+  if (mode == MODE_FWD) return configure_one<KY, MODE_FWD, MAXT>(smem);
+  if (mode == MODE_REC) return configure_one<KY, MODE_REC, MAXT>(smem);
+  return configure_one<KY, MODE_ADJ, MAXT>(smem);
 }
 
 }  // namespace
@@ -732,6 +746,16 @@ cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem
   }
   if (p.nwarps <= 16) return launch_mode<4, 512>(p, mode, grid, smem, st);
   return launch_mode<4, 1024>(p, mode, grid, smem, st);
+}
+
+cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem) {
+  if (smem > 232448) return cudaSuccess;  // a mode this plan never launches
+  if (ky == 8) {
+    if (nwarps <= 12) return configure_mode<8, 384>(mode, smem);
+    return configure_mode<8, 512>(mode, smem);
+  }
+  if (nwarps <= 16) return configure_mode<4, 512>(mode, smem);
+  return configure_mode<4, 1024>(mode, smem);
 }
 
 }  // namespace fdtd

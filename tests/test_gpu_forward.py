@@ -261,3 +261,31 @@ def test_simulate_sources_arc_firing_matches_per_step_form(tb):
     stepped, snaps = tb.simulate_sources(solver, sampler, tx.rows, tx.cols, values, nt, snapshot_steps=(nt - 1,))
     assert rel(fused, stepped.cpu().numpy()) < 1e-6
     assert set(snaps) == {nt - 1}
+
+
+def test_graph_replay_matches_eager_launches(tb):
+    """The forward / adjoint launch sequences replayed as CUDA graphs give the bits
+    of host-launched kernels, also after the output buffers change."""
+    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan, residual_misfit
+    ny, nx, S, nt = 150, 133, 3, 53
+    p = _random_problem(ny, nx, S, 20, nt, seed=21)
+    medium = DeviceMedium(p["c"], p["dx"], p["dy"], p["dt"], "cuda")
+    waves = torch.as_tensor(p["waves"], dtype=torch.float32, device="cuda")
+    src = (p["srow"], p["scol"], p["sw"], p["wave"])
+    rx = (p["row0"], p["col0"], p["w"])
+    out = {}
+    for eager in (1, 0):
+        plan = FusedPlan(medium, rx, src, waves, nt, for_gradient=True,
+                         tuning={"steps_per_launch": 6, "eager": eager})
+        runs = []
+        for _ in range(3):  # fresh output buffers every call: a new graph each time
+            tr = plan.forward(save_checkpoints=True)
+            res, _ = residual_misfit(tr, torch.zeros_like(tr), None)
+            g = torch.zeros((ny, medium.pitch), dtype=torch.float64, device="cuda")
+            plan.adjoint(res, g)
+            runs.append((tr.clone(), g))
+        trs = [r[0] for r in runs]
+        assert all(torch.equal(trs[0], t) for t in trs[1:])
+        out[eager] = runs[0]
+    assert torch.equal(out[0][0], out[1][0])
+    assert rel(out[0][1].cpu().numpy(), out[1][1].cpu().numpy()) < 1e-12
