@@ -107,20 +107,49 @@ def dist_env():
     return world, rank, local
 
 
-def cpu_sample(acq, n_shots=2, n_steps=240):
-    """Time the oracle port (NumPy, float32, one thread) on a bounded sample of the workload."""
+def _oracle_shots(job):
+    """One worker's share of the CPU sample: the oracle port's batched forward on its shots."""
     sys.path.insert(0, str(ROOT))
     from oracle import fdtd_oracle as orc
+    c, dx, dt, geo, fields, wave, n_steps = job
+    orc.simulate_shots_batch(c, dx, dx, dt, geo, fields, wave, n_steps, dtype=np.float32)
+    return fields.shape[0]
+
+
+def cpu_workers():
+    """Host cores available to this process."""
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except AttributeError:
+        return max(1, os.cpu_count() or 1)
+
+
+def make_cpu_pool(workers):
+    """Process pool for the CPU sample, started with spawn (safe beside a CUDA context)."""
+    import multiprocessing as mp
+    return mp.get_context("spawn").Pool(workers)
+
+
+def cpu_sample(acq, pool, workers, shots_per_worker=1, n_steps=480):
+    """Time the oracle port (NumPy, float32) on a bounded sample of the workload, one
+    process per host core, each advancing its own shots (shots are independent)."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import fdtd_oracle as orc
+    n_shots = min(acq.n_shots, workers * shots_per_worker)
     sub = acq.subset(n_shots=n_shots, n_steps=n_steps)
     rows, cols, w, _ = sub.source_tables()
     fields = orc.point_sources(sub.c.shape, rows, cols, w)
     geo = orc.ring_geometry(sub.n_elements, 0.45 * sub.n * sub.dx, sub.x, sub.x)
+    chunks = [c for c in np.array_split(np.arange(n_shots), workers) if c.size]
+    jobs = [(sub.c, sub.dx, sub.dt, geo, fields[c], sub.wavelet[:n_steps], n_steps) for c in chunks]
+    pool.map(_oracle_shots, jobs[:1])  # workers up
     t0 = time.perf_counter()
-    orc.simulate_shots_batch(sub.c, sub.dx, sub.dx, sub.dt, geo, fields, sub.wavelet[:n_steps], n_steps,
-                             dtype=np.float32)
+    done = sum(pool.map(_oracle_shots, jobs))
     dt = time.perf_counter() - t0
-    cells = float(sub.n) ** 2 * n_shots * n_steps
-    return cells / dt / 1e9, f"{n_shots} shots x {n_steps} of {acq.n_steps} steps at {acq.n}^2 (float32 NumPy)"
+    cells = float(sub.n) ** 2 * done * n_steps
+    return (cells / dt / 1e9,
+            f"{done} shots x {n_steps} of {acq.n_steps} steps at {acq.n}^2, {len(jobs)} processes (float32 NumPy)",
+            len(jobs))
 
 
 def run_reference(args):
@@ -130,15 +159,18 @@ def run_reference(args):
     sys.path.insert(0, str(ROOT))
     from soundwavesimulation_gb300.phantoms import config
     acq = config(2)[0]
+    workers = cpu_workers()
+    pool = make_cpu_pool(workers)
     for _ in range(args.warmup):
-        cpu_sample(acq, n_shots=1, n_steps=40)
+        cpu_sample(acq, pool, workers, n_steps=20)
     vals = []
     t0 = time.perf_counter()
-    sample = ""
+    sample, cores = "", workers
     for _ in range(args.steps):
-        v, sample = cpu_sample(acq)
+        v, sample, cores = cpu_sample(acq, pool, workers)
         vals.append(v)
     wall = time.perf_counter() - t0
+    pool.close()
     value = float(np.mean(vals))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -146,7 +178,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded abdomen-like phantom)",
         "config": {"workload": "batched forward 512x512, 128 shots, 4000 steps (bounded CPU sample)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -369,7 +401,10 @@ def run_ours(args):
     traffic = FWD_TRAFFIC.get(shape) if (n, S) == (512, 128) else None
     out = None
     if rank == 0:
-        cpu_v, cpu_s = cpu_sample(acq)
+        workers = cpu_workers()
+        pool = make_cpu_pool(workers)
+        cpu_v, cpu_s, cpu_cores = cpu_sample(acq, pool, workers)
+        pool.close()
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -389,7 +424,7 @@ def run_ours(args):
                       "speedup": value / world / plain_value, "bitwise_equal_traces": same},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": d2h},
-            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port", "sample": cpu_s},
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_cores, "kind": "port", "sample": cpu_s},
             "grad": grad,
             "gpu_launches": launches_per_pass * args.steps,
             "clocks": clocks.summary(),
