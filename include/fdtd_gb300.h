@@ -278,6 +278,21 @@ int32_t fdtd_forward_plain_static(const fdtd_problem* problem, float* traces, vo
 int32_t fdtd_tile_axis(int32_t n, int32_t region, int32_t align, int32_t halo,
                        int32_t band, int32_t max_tiles, int32_t* out, int32_t* n_tiles);
 
+/* Uneven batches: several bound plans (grids of different sizes, step counts and
+   steps per launch, but one rows_per_lane / warps shape) advanced together; each
+   round merges the next temporally blocked launch of every plan into one launch
+   per kernel mode, so small grids share the GPU instead of running one after
+   another. traces / residuals / grads hold one pointer per plan (as for
+   fdtd_forward / fdtd_adjoint); the device workspace (size from
+   fdtd_group_workspace_bytes) holds the launches' parameter tables. Engine-
+   specific: the reference runs the stages of its multiscale driver in turn
+   (invert_ring.py:1037-1045). */
+size_t fdtd_group_workspace_bytes(fdtd_plan* const* plans, int32_t n);
+int32_t fdtd_group_forward(fdtd_plan* const* plans, int32_t n, float* const* traces, int32_t save_checkpoints,
+                           void* workspace, size_t bytes, void* stream);
+int32_t fdtd_group_adjoint(fdtd_plan* const* plans, int32_t n, const float* const* residuals,
+                           double* const* grads, void* workspace, size_t bytes, void* stream);
+
 /* ------------------------------------------------- inversion helpers */
 
 /* Adds the Tikhonov (1/2 alpha ||grad m||^2) and smoothed total-variation

@@ -70,6 +70,11 @@ _SIGNATURES = {
     "fdtd_plan_workspace_bytes": (c_int32, [c_void_p, POINTER(c_size_t)]),
     "fdtd_plan_tuning": (c_int32, [c_void_p, POINTER(Tuning)]),
     "fdtd_plan_bind": (c_int32, [c_void_p, c_void_p, c_size_t, c_void_p]),
+    "fdtd_group_workspace_bytes": (c_size_t, [ctypes.POINTER(c_void_p), c_int32]),
+    "fdtd_group_forward": (c_int32, [ctypes.POINTER(c_void_p), c_int32, ctypes.POINTER(c_void_p), c_int32,
+                                     c_void_p, c_size_t, c_void_p]),
+    "fdtd_group_adjoint": (c_int32, [ctypes.POINTER(c_void_p), c_int32, ctypes.POINTER(c_void_p),
+                                     ctypes.POINTER(c_void_p), c_void_p, c_size_t, c_void_p]),
     "fdtd_regularization": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_double, c_double, c_double,
                                       c_void_p, c_void_p, c_void_p]),
     "fdtd_project": (c_int32, [ctypes.c_int64, c_void_p, c_void_p, c_double, c_double, c_double, c_void_p]),

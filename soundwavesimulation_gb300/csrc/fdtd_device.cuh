@@ -161,6 +161,13 @@ struct TbParams {
   double scale;
 };
 
+// Several plans of one launch shape advanced by one launch (uneven batches).
+struct TbGroup {
+  const TbParams* params;  // (nplans) device array
+  const int* item_off;     // (nplans + 1) prefix sums of tiles * shots
+  int nplans, nitems;
+};
+
 // Dynamic shared-memory carve-up of the temporally blocked kernel; the host
 // sizes the launch with the same function.
 struct TbSmem {

@@ -19,6 +19,11 @@ int32_t cuda_fail(cudaError_t e, const char* what);
 cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st);
 // Sets the dynamic shared-memory attribute of the kernel a launch would use.
 cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem);
+// One launch over the items of several plans (same rows per lane and warps).
+cudaError_t tb_group_launch(const TbGroup& g, int ky, int nwarps, int mode, int grid, size_t smem,
+                            cudaStream_t st);
+// Static shared memory of the grouped kernel (its copy of one plan's parameters).
+size_t tb_group_static_smem();
 
 // One-step kernels and helpers (fdtd_kernels.cu).
 struct StepArgs {

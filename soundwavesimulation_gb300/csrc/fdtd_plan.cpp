@@ -786,12 +786,92 @@ int32_t run_graphed(fdtd_plan* p, fdtd_plan::Graph& g, const void* const (&key)[
   return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "graph launch");
 }
 
+// One stream operation of a pass: a temporally blocked launch or a helper.
+struct Op {
+  enum Kind { LAUNCH, MEMSET, QUANT, DEQUANT } kind = LAUNCH;
+  int mode = 0;
+  TbParams q;
+  void* dst = nullptr;
+  const void* src = nullptr;
+  size_t bytes = 0;
+  float* scales = nullptr;
+  const float* cscales = nullptr;
+  int n_shots = 0;
+  long long per_shot = 0;
+  int store = 0;
+};
+
+int32_t exec_helper(const Op& op, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (op.kind == Op::MEMSET) e = cudaMemsetAsync(op.dst, 0, op.bytes, st);
+  else if (op.kind == Op::QUANT)
+    e = quantize_launch(static_cast<const float*>(op.src), op.dst, op.scales, op.n_shots, op.per_shot, op.store, st);
+  else if (op.kind == Op::DEQUANT)
+    e = dequantize_launch(op.src, op.cscales, static_cast<float*>(op.dst), op.n_shots, op.per_shot, op.store, st);
+  return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "pass helper");
+}
+
+// Where a pass's operations go: straight onto a stream, or into a list (to be
+// merged with other plans' passes into shared launches).
+struct Sink {
+  fdtd_plan* p;
+  cudaStream_t st;
+  std::vector<Op>* rec;
+  int32_t emit(const Op& op) {
+    if (rec) {
+      rec->push_back(op);
+      return FDTD_OK;
+    }
+    if (op.kind == Op::LAUNCH) {
+      TbParams q = op.q;
+      return launch(p, q, op.mode, st);
+    }
+    return exec_helper(op, st);
+  }
+  int32_t launch_tb(int mode, const TbParams& q) {
+    Op op;
+    op.kind = Op::LAUNCH;
+    op.mode = mode;
+    op.q = q;
+    return emit(op);
+  }
+  int32_t memset(void* dst, size_t bytes) {
+    Op op;
+    op.kind = Op::MEMSET;
+    op.dst = dst;
+    op.bytes = bytes;
+    return emit(op);
+  }
+  int32_t quant(const float* src, void* dst, float* scales, int n_shots, long long per_shot, int store) {
+    Op op;
+    op.kind = Op::QUANT;
+    op.src = src;
+    op.dst = dst;
+    op.scales = scales;
+    op.n_shots = n_shots;
+    op.per_shot = per_shot;
+    op.store = store;
+    return emit(op);
+  }
+  int32_t dequant(const void* src, const float* scales, float* dst, int n_shots, long long per_shot, int store) {
+    Op op;
+    op.kind = Op::DEQUANT;
+    op.src = src;
+    op.cscales = scales;
+    op.dst = dst;
+    op.n_shots = n_shots;
+    op.per_shot = per_shot;
+    op.store = store;
+    return emit(op);
+  }
+};
+
 int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u_out,
-                        int32_t save_checkpoints, cudaStream_t st) {
+                        int32_t save_checkpoints, Sink& k) {
   const size_t fb = p->field_elems * sizeof(float);
-  cudaError_t e = cudaMemsetAsync(p->ws + p->o_state[0][0], 0, fb, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(p->ws + p->o_state[0][1], 0, fb, st);
-  if (e != cudaSuccess) return cuda_fail(e, "state reset");
+  int32_t rc0 = k.memset(p->ws + p->o_state[0][0], fb);
+  if (!rc0) rc0 = k.memset(p->ws + p->o_state[0][1], fb);
+  if (rc0) return rc0;
   TbParams q;
   fill_params(p, q);
   q.traces = traces;
@@ -823,7 +903,7 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
     q.out_cur = out_cur;
     q.n0 = n0;
     q.nsteps = ns;
-    int32_t rc = launch(p, q, MODE_FWD, st);
+    int32_t rc = k.launch_tb(MODE_FWD, q);
     if (rc) return rc;
     if (ckpt && p->tun.ckpt_store != FDTD_STORE_F32) {
       const size_t eb = p->field_elems * p->ckpt_elem_bytes;
@@ -831,8 +911,8 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
       for (int f = 0; f < 2; ++f) {
         char* dst = p->ws + p->o_ckpt + ((size_t)(j - 1) * 2 + f) * eb;
         float* sc = fptr(p, p->o_scales) + ((size_t)(j - 1) * 2 + f) * 2 * p->prob.n_shots;
-        e = quantize_launch(f == 0 ? out_prev : out_cur, dst, sc, p->prob.n_shots, per_shot, p->tun.ckpt_store, st);
-        if (e != cudaSuccess) return cuda_fail(e, "checkpoint quantise");
+        rc = k.quant(f == 0 ? out_prev : out_cur, dst, sc, p->prob.n_shots, per_shot, p->tun.ckpt_store);
+        if (rc) return rc;
       }
     }
     in_prev = out_prev;
@@ -842,11 +922,11 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
   return FDTD_OK;
 }
 
-int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, cudaStream_t st) {
+int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Sink& k) {
   const size_t fb = p->field_elems * sizeof(float);
-  cudaError_t e = cudaMemsetAsync(p->ws + p->o_adj[0][0], 0, fb, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(p->ws + p->o_adj[0][1], 0, fb, st);
-  if (e != cudaSuccess) return cuda_fail(e, "adjoint reset");
+  int32_t rc0 = k.memset(p->ws + p->o_adj[0][0], fb);
+  if (!rc0) rc0 = k.memset(p->ws + p->o_adj[0][1], fb);
+  if (rc0) return rc0;
   TbParams q;
   fill_params(p, q);
   q.residual = residual;
@@ -862,9 +942,9 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, cu
     const float* in_cur;
     int in_set;
     if (j == 0) {
-      e = cudaMemsetAsync(p->ws + p->o_state[0][0], 0, fb, st);
-      if (e == cudaSuccess) e = cudaMemsetAsync(p->ws + p->o_state[0][1], 0, fb, st);
-      if (e != cudaSuccess) return cuda_fail(e, "recompute reset");
+      int32_t rc = k.memset(p->ws + p->o_state[0][0], fb);
+      if (!rc) rc = k.memset(p->ws + p->o_state[0][1], fb);
+      if (rc) return rc;
       in_prev = fptr(p, p->o_state[0][0]);
       in_cur = fptr(p, p->o_state[0][1]);
       in_set = 0;
@@ -878,9 +958,9 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, cu
       for (int f = 0; f < 2; ++f) {
         const char* src = p->ws + p->o_ckpt + ((size_t)(j - 1) * 2 + f) * eb;
         const float* sc = fptr(p, p->o_scales) + ((size_t)(j - 1) * 2 + f) * 2 * p->prob.n_shots;
-        e = dequantize_launch(src, sc, fptr(p, p->o_state[0][f]), p->prob.n_shots, per_shot,
-                              p->tun.ckpt_store, st);
-        if (e != cudaSuccess) return cuda_fail(e, "checkpoint dequantise");
+        const int32_t rc = k.dequant(src, sc, fptr(p, p->o_state[0][f]), p->prob.n_shots, per_shot,
+                                     p->tun.ckpt_store);
+        if (rc) return rc;
       }
       in_prev = fptr(p, p->o_state[0][0]);
       in_cur = fptr(p, p->o_state[0][1]);
@@ -897,7 +977,7 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, cu
       q.out_cur = fptr(p, p->o_state[out_set][1]);
       q.n0 = n0;
       q.nsteps = ns;
-      int32_t rc = launch(p, q, MODE_REC, st);
+      int32_t rc = k.launch_tb(MODE_REC, q);
       if (rc) return rc;
       in_prev = q.out_prev;
       in_cur = q.out_cur;
@@ -913,7 +993,7 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, cu
       q.out_cur = fptr(p, p->o_adj[out][1]);
       q.n0 = ntop;
       q.nsteps = ns;
-      int32_t rc = launch(p, q, MODE_ADJ, st);
+      int32_t rc = k.launch_tb(MODE_ADJ, q);
       if (rc) return rc;
       adj_in = out;
     }
@@ -921,9 +1001,173 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, cu
   return FDTD_OK;
 }
 
+// ---- several plans in shared launches (uneven batches: grids of different
+// sizes, steps and temporal-block depths, one launch shape)
+
+struct GroupAction {
+  int helper_plan = -1;      // >= 0: one helper op of that plan
+  size_t helper_op = 0;
+  int mode = 0;              // else: one shared launch of `members`
+  std::vector<std::pair<int, size_t>> members;
+};
+
+size_t group_launch_bound(fdtd_plan* const* plans, int n) {
+  size_t launches = 0;
+  for (int i = 0; i < n; ++i) {
+    const fdtd_plan* p = plans[i];
+    const size_t per_pass = (size_t)(p->prob.n_steps + p->tmax - 1) / p->tmax;
+    const size_t per_seg = (size_t)(p->ckpt_every + p->tmax - 1) / p->tmax;
+    launches += std::max(per_pass, (size_t)p->nseg * 2 * per_seg);
+  }
+  return launches;
+}
+
+size_t group_bytes(fdtd_plan* const* plans, int n) {
+  const size_t L = group_launch_bound(plans, n);
+  return align_up(L * sizeof(TbParams)) + align_up(L * (size_t)(n + 1) * sizeof(int));
+}
+
+template <typename F>
+int32_t group_run(fdtd_plan* const* plans, int n, void* workspace, size_t bytes, cudaStream_t st, F enqueue) {
+  if (!plans || n < 1) return fail(FDTD_ERR_INVALID, "group: no plans");
+  for (int i = 0; i < n; ++i) {
+    if (!plans[i] || !plans[i]->bound) return fail(FDTD_ERR_STATE, "group: every plan must be bound");
+    if (plans[i]->ky != plans[0]->ky || plans[i]->nw != plans[0]->nw)
+      return fail(FDTD_ERR_UNSUPPORTED, "group: plans must share rows_per_lane and warps");
+  }
+  if (!workspace || bytes < group_bytes(plans, n)) return fail(FDTD_ERR_WORKSPACE, "group: workspace too small");
+  // every plan's pass as a list of operations
+  std::vector<std::vector<Op>> ops(n);
+  for (int i = 0; i < n; ++i) {
+    Sink k{plans[i], st, &ops[i]};
+    const int32_t rc = enqueue(plans[i], k);
+    if (rc) return rc;
+  }
+  // rounds: each plan runs its helpers up to its next launch; the next launches of
+  // all plans form one shared launch per mode
+  std::vector<size_t> idx(n, 0);
+  std::vector<GroupAction> acts;
+  for (;;) {
+    bool left = false;
+    for (int i = 0; i < n; ++i) {
+      while (idx[i] < ops[i].size() && ops[i][idx[i]].kind != Op::LAUNCH) {
+        GroupAction a;
+        a.helper_plan = i;
+        a.helper_op = idx[i]++;
+        acts.push_back(a);
+      }
+      left = left || idx[i] < ops[i].size();
+    }
+    if (!left) break;
+    for (int m = 0; m < 3; ++m) {
+      GroupAction a;
+      a.mode = m;
+      for (int i = 0; i < n; ++i)
+        if (idx[i] < ops[i].size() && ops[i][idx[i]].mode == m) a.members.push_back({i, idx[i]});
+      if (a.members.empty()) continue;
+      for (auto& mb : a.members) ++idx[mb.first];
+      acts.push_back(a);
+    }
+  }
+  // parameters and item offsets of the shared launches, uploaded at once
+  std::vector<TbParams> hp;
+  std::vector<int> hoff;
+  for (const GroupAction& a : acts) {
+    if (a.helper_plan >= 0 || a.members.size() < 2) continue;
+    int items = 0;
+    for (auto& mb : a.members) {
+      hp.push_back(ops[mb.first][mb.second].q);
+      hoff.push_back(items);
+      items += plans[mb.first]->prob.n_shots * (int)plans[mb.first]->tiles.size();
+    }
+    hoff.push_back(items);
+  }
+  const size_t L = group_launch_bound(plans, n);
+  if (hp.size() > L || hoff.size() > L * (size_t)(n + 1)) return fail(FDTD_ERR_UNSUPPORTED, "group: launch bound exceeded");
+  char* dws = static_cast<char*>(workspace);
+  TbParams* dparams = reinterpret_cast<TbParams*>(dws);
+  int* doff = reinterpret_cast<int*>(dws + align_up(L * sizeof(TbParams)));
+  cudaError_t e = cudaSuccess;
+  if (!hp.empty()) e = cudaMemcpyAsync(dparams, hp.data(), hp.size() * sizeof(TbParams), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !hoff.empty())
+    e = cudaMemcpyAsync(doff, hoff.data(), hoff.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e, "group parameter upload");
+  size_t pk = 0, ok = 0;
+  for (const GroupAction& a : acts) {
+    if (a.helper_plan >= 0) {
+      const int32_t rc = exec_helper(ops[a.helper_plan][a.helper_op], st);
+      if (rc) return rc;
+      continue;
+    }
+    if (a.members.size() == 1) {
+      fdtd_plan* p = plans[a.members[0].first];
+      TbParams q = ops[a.members[0].first][a.members[0].second].q;
+      const int32_t rc = launch(p, q, a.mode, st);
+      if (rc) return rc;
+      continue;
+    }
+    size_t smem = 0;
+    int items = 0;
+    for (auto& mb : a.members) {
+      smem = std::max(smem, plans[mb.first]->smem[a.mode]);
+      items += plans[mb.first]->prob.n_shots * (int)plans[mb.first]->tiles.size();
+    }
+    if (smem + tb_group_static_smem() > SMEM_LIMIT) return fail(FDTD_ERR_UNSUPPORTED, "group: shared memory need exceeds 227 KB");
+    TbGroup g;
+    g.params = dparams + pk;
+    g.item_off = doff + ok;
+    g.nplans = (int)a.members.size();
+    g.nitems = items;
+    const int grid = std::max(1, std::min(items, plans[0]->sm_count * std::max(1, plans[0]->tun.ctas_per_sm)));
+    e = tb_group_launch(g, plans[0]->ky, plans[0]->nw, a.mode, grid, smem, st);
+    if (e != cudaSuccess) return cuda_fail(e, "grouped kernel launch");
+    pk += a.members.size();
+    ok += a.members.size() + 1;
+  }
+  return FDTD_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+size_t fdtd_group_workspace_bytes(fdtd_plan* const* plans, int32_t n) {
+  if (!plans || n < 1) return 0;
+  for (int i = 0; i < n; ++i)
+    if (!plans[i]) return 0;
+  return group_bytes(plans, n);
+}
+
+int32_t fdtd_group_forward(fdtd_plan* const* plans, int32_t n, float* const* traces, int32_t save_checkpoints,
+                           void* workspace, size_t bytes, void* stream) {
+  if (!traces) return fail(FDTD_ERR_INVALID, "group: traces must be set");
+  for (int i = 0; i < n; ++i) {
+    if (!traces[i]) return fail(FDTD_ERR_INVALID, "group: traces must be set");
+    if (plans && plans[i] && save_checkpoints && !plans[i]->for_gradient)
+      return fail(FDTD_ERR_STATE, "group: a plan was created without gradient storage");
+  }
+  int k = 0;
+  const int32_t rc = group_run(plans, n, workspace, bytes, (cudaStream_t)stream, [&](fdtd_plan* p, Sink& s) {
+    return forward_enqueue(p, traces[k++], nullptr, nullptr, save_checkpoints, s);
+  });
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i) plans[i]->have_ckpt = save_checkpoints != 0;
+  return FDTD_OK;
+}
+
+int32_t fdtd_group_adjoint(fdtd_plan* const* plans, int32_t n, const float* const* residuals, double* const* grads,
+                           void* workspace, size_t bytes, void* stream) {
+  if (!residuals || !grads) return fail(FDTD_ERR_INVALID, "group: residuals and gradients must be set");
+  for (int i = 0; i < n; ++i) {
+    if (!residuals[i] || !grads[i]) return fail(FDTD_ERR_INVALID, "group: residuals and gradients must be set");
+    if (plans && plans[i] && !plans[i]->have_ckpt) return fail(FDTD_ERR_STATE, "group: run the forward with checkpoints first");
+  }
+  int k = 0;
+  return group_run(plans, n, workspace, bytes, (cudaStream_t)stream, [&](fdtd_plan* p, Sink& s) {
+    const int j = k++;
+    return adjoint_enqueue(p, residuals[j], grads[j], s);
+  });
+}
 
 int32_t fdtd_forward(fdtd_plan* p, float* traces, float* u_prev_out, float* u_out,
                      int32_t save_checkpoints, void* stream) {
@@ -934,7 +1178,8 @@ int32_t fdtd_forward(fdtd_plan* p, float* traces, float* u_prev_out, float* u_ou
   const void* const key[4] = {traces, u_prev_out, u_out, nullptr};
   const int32_t rc = run_graphed(p, p->g_fwd, key, save_checkpoints != 0, (cudaStream_t)stream,
                                  [&](cudaStream_t st) {
-                                   return forward_enqueue(p, traces, u_prev_out, u_out, save_checkpoints, st);
+                                   Sink k{p, st, nullptr};
+                                   return forward_enqueue(p, traces, u_prev_out, u_out, save_checkpoints, k);
                                  });
   if (rc) return rc;
   p->have_ckpt = save_checkpoints != 0;
@@ -947,7 +1192,10 @@ int32_t fdtd_adjoint(fdtd_plan* p, const float* residual, double* grad_c2, void*
   if (!residual || !grad_c2) return fail(FDTD_ERR_INVALID, "null pointer");
   const void* const key[4] = {residual, grad_c2, nullptr, nullptr};
   return run_graphed(p, p->g_adj, key, 0, (cudaStream_t)stream,
-                     [&](cudaStream_t st) { return adjoint_enqueue(p, residual, grad_c2, st); });
+                     [&](cudaStream_t st) {
+                       Sink k{p, st, nullptr};
+                       return adjoint_enqueue(p, residual, grad_c2, k);
+                     });
 }
 
 // ----------------------------------------------------------- plain engine

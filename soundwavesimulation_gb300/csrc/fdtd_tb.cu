@@ -487,35 +487,32 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
   }
 }
 
-template <int KY, int MODE, int MAXT>
-__global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int nw = p.nwarps;
-  const int nthr = nw * 32;
-  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef, p.nsrow_max);
-  Ctx x;
-  x.tid = threadIdx.x;
-  x.w = x.tid >> 5;
-  x.lane = x.tid & 31;
-  x.nw = nw;
+// Binds the context's shared-memory carve-up for the launch parameters `p`.
+template <int KY, int MODE>
+__device__ __forceinline__ void bind_ctx(const TbParams& p, Ctx& x, unsigned char* smem) {
+  const TbSmem L = tb_smem_layout(p.nwarps, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef, p.nsrow_max);
+  x.nw = p.nwarps;
   x.s_coef = reinterpret_cast<float*>(smem + L.coef);
   x.s_lap = reinterpret_cast<float*>(smem + L.lap);
   x.s_g = reinterpret_cast<float*>(smem + L.g);
   x.s_xch = reinterpret_cast<float4*>(smem + L.xch);
   x.s_mur = reinterpret_cast<float*>(smem + L.mur);
   x.s_tap = reinterpret_cast<float*>(smem + L.tap);
+  x.s_src = reinterpret_cast<float*>(smem + L.src);
+}
+
+// One (tile, shot) item: load, T steps, store, traces / gradient flush.
+template <int KY, int MODE>
+__device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char* smem, int item) {
+  const int nw = p.nwarps;
+  const int nthr = nw * 32;
+  const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef, p.nsrow_max);
   float* s_res = reinterpret_cast<float*>(smem + L.res);
   unsigned* s_mask = reinterpret_cast<unsigned*>(smem + L.mask);
   int* s_base = reinterpret_cast<int*>(smem + L.base);
   unsigned* s_smask = reinterpret_cast<unsigned*>(smem + L.smask);
   int* s_sbase = reinterpret_cast<int*>(smem + L.sbase);
-  x.s_src = reinterpret_cast<float*>(smem + L.src);
-  const int nitems = p.ntiles * p.nshots;
-
-  // Items are (tile, shot) pairs with shots varying fastest, dealt out with a
-  // grid stride: at any moment the CTAs hold a mix of edge, interior and
-  // receiver-heavy tiles, which balances better than contiguous runs per CTA.
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+  {
     const int ti = item / p.nshots;
     const int s = item - ti * p.nshots;
     const TbTile t = p.tiles[ti];
@@ -701,6 +698,49 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
 }
 
 template <int KY, int MODE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Ctx x;
+  x.tid = threadIdx.x;
+  x.w = x.tid >> 5;
+  x.lane = x.tid & 31;
+  bind_ctx<KY, MODE>(p, x, smem);
+  const int nitems = p.ntiles * p.nshots;
+  // Items are (tile, shot) pairs with shots varying fastest, dealt out with a
+  // grid stride: at any moment the CTAs hold a mix of edge, interior and
+  // receiver-heavy tiles, which balances better than contiguous runs per CTA.
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) run_one<KY, MODE>(p, x, smem, item);
+}
+
+// Several plans (grids) of one launch shape in one launch: the items of plan i
+// are [item_off[i], item_off[i+1]); a CTA copies the parameters of the plan of
+// its current item into shared memory when the plan changes.
+template <int KY, int MODE, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) tb_group_kernel(const TbGroup g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(16) TbParams sp;
+  Ctx x;
+  x.tid = threadIdx.x;
+  x.w = x.tid >> 5;
+  x.lane = x.tid & 31;
+  int cur = -1;
+  for (int item = blockIdx.x; item < g.nitems; item += gridDim.x) {
+    int pi = 0;
+    while (pi + 1 < g.nplans && item >= __ldg(g.item_off + pi + 1)) ++pi;
+    if (pi != cur) {
+      __syncthreads();
+      const int* src = reinterpret_cast<const int*>(g.params + pi);
+      int* dst = reinterpret_cast<int*>(&sp);
+      for (int i = x.tid; i < (int)(sizeof(TbParams) / sizeof(int)); i += blockDim.x) dst[i] = __ldg(src + i);
+      __syncthreads();
+      bind_ctx<KY, MODE>(sp, x, smem);
+      cur = pi;
+    }
+    run_one<KY, MODE>(sp, x, smem, item - __ldg(g.item_off + pi));
+  }
+}
+
+template <int KY, int MODE, int MAXT>
 cudaError_t configure_one(size_t smem) {
   static size_t configured_smem = 0;  // per device it is the same binary; raise only
   if (smem > configured_smem) {
@@ -747,6 +787,38 @@ cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem
   if (p.nwarps <= 16) return launch_mode<4, 512>(p, mode, grid, smem, st);
   return launch_mode<4, 1024>(p, mode, grid, smem, st);
 }
+
+template <int KY, int MODE, int MAXT>
+cudaError_t group_one(const TbGroup& g, int nwarps, int grid, size_t smem, cudaStream_t st) {
+  static size_t configured_smem = 0;
+  if (smem > configured_smem) {
+    cudaError_t e = cudaFuncSetAttribute(tb_group_kernel<KY, MODE, MAXT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured_smem = smem;
+  }
+  tb_group_kernel<KY, MODE, MAXT><<<grid, nwarps * 32, smem, st>>>(g);
+  return cudaGetLastError();
+}
+
+template <int KY, int MAXT>
+cudaError_t group_mode(const TbGroup& g, int nwarps, int mode, int grid, size_t smem, cudaStream_t st) {
+  if (mode == MODE_FWD) return group_one<KY, MODE_FWD, MAXT>(g, nwarps, grid, smem, st);
+  if (mode == MODE_REC) return group_one<KY, MODE_REC, MAXT>(g, nwarps, grid, smem, st);
+  return group_one<KY, MODE_ADJ, MAXT>(g, nwarps, grid, smem, st);
+}
+
+cudaError_t tb_group_launch(const TbGroup& g, int ky, int nwarps, int mode, int grid, size_t smem,
+                            cudaStream_t st) {
+  if (ky == 8) {
+    if (nwarps <= 12) return group_mode<8, 384>(g, nwarps, mode, grid, smem, st);
+    return group_mode<8, 512>(g, nwarps, mode, grid, smem, st);
+  }
+  if (nwarps <= 16) return group_mode<4, 512>(g, nwarps, mode, grid, smem, st);
+  return group_mode<4, 1024>(g, nwarps, mode, grid, smem, st);
+}
+
+size_t tb_group_static_smem() { return sizeof(TbParams) + 16; }
 
 cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem) {
   if (smem > 232448) return cudaSuccess;  // a mode this plan never launches

@@ -219,6 +219,48 @@ class FusedPlan(ProblemTables):
             pass
 
 
+class PlanGroup:
+    """Several FusedPlans (grids of different sizes and step counts, one launch
+    shape) advanced together: each round of temporally blocked launches runs as
+    one launch per kernel mode over the items of every plan."""
+
+    def __init__(self, plans):
+        self.plans = list(plans)
+        if not self.plans:
+            raise ValueError("a group needs at least one plan")
+        dev = self.plans[0].medium.device
+        if any(p.medium.device != dev for p in self.plans):
+            raise ValueError("all plans of a group must live on one device")
+        self.device = dev
+        self.lib = _lib.load()
+        self._handles = (ctypes.c_void_p * len(self.plans))(*[p._plan.value for p in self.plans])
+        nbytes = int(self.lib.fdtd_group_workspace_bytes(self._handles, len(self.plans)))
+        if nbytes == 0:
+            raise ValueError("invalid plan group")
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+
+    def _ptrs(self, tensors):
+        return (ctypes.c_void_p * len(tensors))(*[ptr(t) for t in tensors])
+
+    def forward(self, traces=None, save_checkpoints=False):
+        """All plans' forward passes; returns the list of traces (S, R, nt) per plan."""
+        if traces is None:
+            traces = [torch.empty((p.n_shots, p.n_rx, p.n_steps), dtype=torch.float32, device=self.device)
+                      for p in self.plans]
+        for p in self.plans:
+            p.refresh_medium()
+        _lib.check(self.lib.fdtd_group_forward(self._handles, len(self.plans), self._ptrs(traces),
+                                               int(bool(save_checkpoints)), ptr(self.workspace),
+                                               self.workspace.numel(), stream_handle(self.device)), "group forward")
+        return traces
+
+    def adjoint(self, residuals, grads):
+        """All plans' checkpointed adjoints; grads[i] float64 (ny, pitch) of plan i accumulate."""
+        _lib.check(self.lib.fdtd_group_adjoint(self._handles, len(self.plans), self._ptrs(residuals),
+                                               self._ptrs(grads), ptr(self.workspace), self.workspace.numel(),
+                                               stream_handle(self.device)), "group adjoint")
+
+
 def residual_misfit(traces, observed, mute, residual=None, misfit=None):
     """residual = traces - observed (muted channel per shot) and 0.5 * sum(residual^2) in float64."""
     lib = _lib.load()
