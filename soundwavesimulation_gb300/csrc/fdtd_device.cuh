@@ -192,7 +192,7 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
     m.lap = off;
     off += region;
   }
-  m.g = off; if (mode == MODE_ADJ) off += region;
+  m.g = off;  // (the adjoint's gradient tile lives in tensor memory)
   m.xch = off; off += size_t(2) * nw * 2 * 32 * 16;
   // Mur table of an edge tile: k set and ratio set, each 2 region heights +
   // 2 region widths + 8 corner values

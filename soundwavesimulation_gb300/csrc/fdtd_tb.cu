@@ -42,7 +42,7 @@ struct Ctx {
   const float* gcoef;       // global coefficients at (y0, xb) (adjoint)
   float* s_coef;
   float* s_lap;
-  float* s_g;
+  unsigned tm;              // adjoint: tensor-memory address of this thread's gradient tile
   float4* s_xch;
   float* s_mur;             // the tile's Mur table (edge tiles)
   float* s_tap;
@@ -72,6 +72,51 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// ---- tensor memory (TMEM) holds the adjoint's gradient tile
+//
+// 128 columns per CTA. Warp w reaches the TMEM lanes of quadrant w % 4 (lane l of
+// the warp is TMEM lane 32 (w % 4) + l) and uses columns 4 KY (w / 4) ..
+// 4 KY (w / 4) + 4 KY - 1: column 4 r + c holds cell (r, c) of the thread. The
+// imaging read-modify-write thus runs through the tensor-memory datapath instead
+// of the shared-memory pipe.
+constexpr unsigned TM_COLS = 128;
+
+__device__ __forceinline__ unsigned smem_u32(const void* ptr) {
+  return (unsigned)__cvta_generic_to_shared(ptr);
+}
+
+__device__ __forceinline__ void tm_alloc(unsigned* dst) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(TM_COLS)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tm_dealloc(unsigned base) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(base), "r"(TM_COLS) : "memory");
+}
+
+__device__ __forceinline__ void tm_fence_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tm_ld8(unsigned addr, unsigned (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(addr)
+               : "memory");
+}
+
+__device__ __forceinline__ void tm_st8(unsigned addr, const unsigned (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(addr),
+               "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+               : "memory");
+}
+
+__device__ __forceinline__ void tm_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Coefficients (c dt)^2 of band row r: from the shared-memory copy of the region
 // or, for an adjoint without room for it, through L1 from global memory; zero
@@ -394,27 +439,42 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
       }
     }
   }
-  if (MODE == MODE_ADJ && x.own_rows && x.own_cols) {
+  if (MODE == MODE_ADJ && x.own_rows) {  // warp-uniform: the tensor-memory ops are warp-wide
     if (n >= 1) {
       // lap(u^{n-1}) of this thread's owned cells was streamed into shared
       // memory (cp.async) during the previous step
       cp_async_wait_all();
+      __syncwarp();  // the tensor-memory instructions need the whole warp converged
+      tm_wait_st();
       const float4* l4 = reinterpret_cast<const float4*>(x.s_lap) + (x.w * KY) * 32 + x.lane;
-      float4* g4 = reinterpret_cast<float4*>(x.s_g) + (x.w * KY) * 32 + x.lane;
 #pragma unroll
-      for (int r = 0; r < KY; ++r) {
-        if ((x.own_rows >> r) & 1u) {
-          // all four columns in pairs: a column this thread does not own sums
-          // whatever its Laplacian slot holds, and is never flushed
-          const float4 lv = l4[r * 32];
-          const float4 gv = g4[r * 32];
-          const float2 ga = __ffma2_rn(make_float2(P[r][0], P[r][1]), make_float2(lv.x, lv.y), make_float2(gv.x, gv.y));
-          const float2 gb = __ffma2_rn(make_float2(P[r][2], P[r][3]), make_float2(lv.z, lv.w), make_float2(gv.z, gv.w));
-          g4[r * 32] = make_float4(ga.x, ga.y, gb.x, gb.y);
+      for (int r = 0; r < KY; r += 2) {
+        if ((x.own_rows >> r) & 3u) {
+          // rows r and r+1, all four columns: a cell this thread does not own
+          // sums whatever its Laplacian slot holds, and is never flushed
+          unsigned v[8];
+          tm_ld8(x.tm + 4 * r, v);
+          const float4 la = l4[r * 32];
+          const float4 lb = l4[(r + 1) * 32];
+          tm_wait_ld();
+          float2 g;
+          g = __ffma2_rn(make_float2(P[r][0], P[r][1]), make_float2(la.x, la.y),
+                         make_float2(__uint_as_float(v[0]), __uint_as_float(v[1])));
+          v[0] = __float_as_uint(g.x); v[1] = __float_as_uint(g.y);
+          g = __ffma2_rn(make_float2(P[r][2], P[r][3]), make_float2(la.z, la.w),
+                         make_float2(__uint_as_float(v[2]), __uint_as_float(v[3])));
+          v[2] = __float_as_uint(g.x); v[3] = __float_as_uint(g.y);
+          g = __ffma2_rn(make_float2(P[r + 1][0], P[r + 1][1]), make_float2(lb.x, lb.y),
+                         make_float2(__uint_as_float(v[4]), __uint_as_float(v[5])));
+          v[4] = __float_as_uint(g.x); v[5] = __float_as_uint(g.y);
+          g = __ffma2_rn(make_float2(P[r + 1][2], P[r + 1][3]), make_float2(lb.z, lb.w),
+                         make_float2(__uint_as_float(v[6]), __uint_as_float(v[7])));
+          v[6] = __float_as_uint(g.x); v[7] = __float_as_uint(g.y);
+          tm_st8(x.tm + 4 * r, v);
         }
       }
     }
-    if (k + 1 < p.nsteps && n - 1 >= 1) prefetch_lap<KY>(p, x, n - 1);
+    if (x.own_cols && k + 1 < p.nsteps && n - 1 >= 1) prefetch_lap<KY>(p, x, n - 1);
   }
 
   // ---- publish the band's first and last rows for the next step
@@ -494,7 +554,6 @@ __device__ __forceinline__ void bind_ctx(const TbParams& p, Ctx& x, unsigned cha
   x.nw = p.nwarps;
   x.s_coef = reinterpret_cast<float*>(smem + L.coef);
   x.s_lap = reinterpret_cast<float*>(smem + L.lap);
-  x.s_g = reinterpret_cast<float*>(smem + L.g);
   x.s_xch = reinterpret_cast<float4*>(smem + L.xch);
   x.s_mur = reinterpret_cast<float*>(smem + L.mur);
   x.s_tap = reinterpret_cast<float*>(smem + L.tap);
@@ -539,7 +598,7 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
     }
 
     // coefficients of the region (zero outside the domain; the padding columns of
-    // coef are zero in memory) and, for the adjoint, a cleared gradient tile
+    // coef are zero in memory)
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
       if (MODE != MODE_ADJ || p.adj_coef) {
@@ -547,9 +606,13 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
         if ((x.rowvalid >> r) & 1u) v = ldg4(x.gcoef + (long long)r * p.pitch);
         reinterpret_cast<float4*>(x.s_coef)[(x.w * KY + r) * 32 + x.lane] = v;
       }
-      if (MODE == MODE_ADJ) {
-        reinterpret_cast<float4*>(x.s_g)[(x.w * KY + r) * 32 + x.lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
+    }
+    if (MODE == MODE_ADJ) {  // cleared gradient tile in tensor memory
+      const unsigned z[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+      __syncwarp();
+      tm_wait_st();
+#pragma unroll
+      for (int c = 0; c < 4 * KY; c += 8) tm_st8(x.tm + c, z);
     }
     if (t.flags) {
       // the tile's Mur table: left / right k per region row, bottom / top per
@@ -674,22 +737,32 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
         p.traces[((long long)s * p.nrx + rc.rg) * p.nt + p.n0 + k] = smp;
       }
     }
-    if (MODE == MODE_ADJ && x.own_rows && x.own_cols) {
-      const float4* g4 = reinterpret_cast<const float4*>(x.s_g) + (x.w * KY) * 32 + x.lane;
+    if (MODE == MODE_ADJ && x.own_rows) {  // warp-uniform: tensor-memory loads are warp-wide
+      __syncwarp();
+      tm_wait_st();
 #pragma unroll
-      for (int r = 0; r < KY; ++r) {
-        if ((x.own_rows >> r) & 1u) {
+      for (int r0 = 0; r0 < KY; r0 += 2) {
+        if (!((x.own_rows >> r0) & 3u)) continue;
+        unsigned v[8];
+        __syncwarp();
+        tm_ld8(x.tm + 4 * r0, v);
+        tm_wait_ld();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int r = r0 + h;
+          if (!x.own_cols || !((x.own_rows >> r) & 1u)) continue;
           // the tile summed w * lap with w = coef * l: divide by coef once here, in
           // float32 (GB300's float64 pipe is ~64x slower); only the cross-item sum
           // (the atomic) is float64
-          const float4 gv = g4[r * 32];
           const float4 co = ldg4(x.gcoef + (long long)r * p.pitch);
           const float sc = (float)p.scale;
+          const float g0 = __uint_as_float(v[4 * h]), g1 = __uint_as_float(v[4 * h + 1]);
+          const float g2 = __uint_as_float(v[4 * h + 2]), g3 = __uint_as_float(v[4 * h + 3]);
           double* gd = p.grad + (long long)(x.y0 + r) * p.pitch + x.xb;
-          if (x.own_cols & 1u) atomicAdd(gd + 0, (double)(__fdiv_rn(gv.x, co.x) * sc));
-          if (x.own_cols & 2u) atomicAdd(gd + 1, (double)(__fdiv_rn(gv.y, co.y) * sc));
-          if (x.own_cols & 4u) atomicAdd(gd + 2, (double)(__fdiv_rn(gv.z, co.z) * sc));
-          if (x.own_cols & 8u) atomicAdd(gd + 3, (double)(__fdiv_rn(gv.w, co.w) * sc));
+          if (x.own_cols & 1u) atomicAdd(gd + 0, (double)(__fdiv_rn(g0, co.x) * sc));
+          if (x.own_cols & 2u) atomicAdd(gd + 1, (double)(__fdiv_rn(g1, co.y) * sc));
+          if (x.own_cols & 4u) atomicAdd(gd + 2, (double)(__fdiv_rn(g2, co.z) * sc));
+          if (x.own_cols & 8u) atomicAdd(gd + 3, (double)(__fdiv_rn(g3, co.w) * sc));
         }
       }
     }
@@ -697,19 +770,43 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
   }
 }
 
+// The adjoint's tensor-memory columns: allocated by warp 0 at kernel start and
+// freed by it at the end; thread address of the gradient tile into x.tm.
+template <int KY, int MODE>
+__device__ __forceinline__ unsigned tm_begin(Ctx& x, unsigned* slot) {
+  if (MODE != MODE_ADJ) return 0;
+  if (x.w == 0) tm_alloc(slot);
+  tm_fence_sync();
+  const unsigned base = *slot;
+  x.tm = base + ((unsigned)(32 * (x.w & 3)) << 16) + (unsigned)(4 * KY * (x.w >> 2));
+  return base;
+}
+
+template <int MODE>
+__device__ __forceinline__ void tm_end(const Ctx& x, unsigned base) {
+  if (MODE != MODE_ADJ) return;
+  __syncwarp();
+  tm_wait_st();
+  tm_fence_sync();
+  if (x.w == 0) tm_dealloc(base);
+}
+
 template <int KY, int MODE, int MAXT>
 __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ unsigned tm_slot;
   Ctx x;
   x.tid = threadIdx.x;
   x.w = x.tid >> 5;
   x.lane = x.tid & 31;
   bind_ctx<KY, MODE>(p, x, smem);
+  const unsigned tm_base = tm_begin<KY, MODE>(x, &tm_slot);
   const int nitems = p.ntiles * p.nshots;
   // Items are (tile, shot) pairs with shots varying fastest, dealt out with a
   // grid stride: at any moment the CTAs hold a mix of edge, interior and
   // receiver-heavy tiles, which balances better than contiguous runs per CTA.
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) run_one<KY, MODE>(p, x, smem, item);
+  tm_end<MODE>(x, tm_base);
 }
 
 // Several plans (grids) of one launch shape in one launch: the items of plan i
@@ -719,10 +816,12 @@ template <int KY, int MODE, int MAXT>
 __global__ void __launch_bounds__(MAXT, 1) tb_group_kernel(const TbGroup g) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(16) TbParams sp;
+  __shared__ unsigned tm_slot;
   Ctx x;
   x.tid = threadIdx.x;
   x.w = x.tid >> 5;
   x.lane = x.tid & 31;
+  const unsigned tm_base = tm_begin<KY, MODE>(x, &tm_slot);
   int cur = -1;
   for (int item = blockIdx.x; item < g.nitems; item += gridDim.x) {
     int pi = 0;
@@ -738,6 +837,7 @@ __global__ void __launch_bounds__(MAXT, 1) tb_group_kernel(const TbGroup g) {
     }
     run_one<KY, MODE>(sp, x, smem, item - __ldg(g.item_off + pi));
   }
+  tm_end<MODE>(x, tm_base);
 }
 
 template <int KY, int MODE, int MAXT>
