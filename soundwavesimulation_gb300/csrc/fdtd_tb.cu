@@ -19,9 +19,16 @@
 //     (fdtd2d/torch_backend.py:563-580), the receiver gather
 //     (fdtd2d/torch_backend.py:540-548), the per-step Laplacian of the forward
 //     field (recompute) and the imaging condition
-//     (fdtd2d/torch_backend.py:583-598) are all applied inside the block.
-// The arithmetic helpers in fdtd_device.cuh make every value bit-identical to
-// the one-step kernels in fdtd_kernels.cu.
+//     (fdtd2d/torch_backend.py:583-598) are all applied inside the block:
+//     receiver taps and source nodes as per-step shared-memory stages of whole
+//     4-cell rows, Mur coefficients from a per-tile shared-memory table, the
+//     adjoint's gradient tile in tensor memory (tcgen05) and its Laplacian
+//     stream one step ahead through cp.async.
+// The stencil runs on cell pairs with the two-lane float32 instructions; like
+// the scalar helpers in fdtd_device.cuh every element is one IEEE
+// round-to-nearest operation, so the values are bit-identical to the one-step
+// kernels in fdtd_kernels.cu. `tb_group_kernel` runs the items of several plans
+// (grids) in one launch.
 
 #include "fdtd_device.cuh"
 #include "fdtd_internal.h"
