@@ -71,11 +71,6 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
@@ -135,26 +130,19 @@ __device__ __forceinline__ float4 coefrow(const TbParams& p, const Ctx& x, const
   return ldg4(x.gcoef + (long long)r * p.pitch);
 }
 
-// Streams lap(u^{n-1}) of this thread's owned cells for adjoint step n into its
-// slots of the shared-memory Laplacian tile.
+// Streams lap(u^{n-1}) of this thread's owned rows for adjoint step n into its
+// slots of the shared-memory Laplacian tile, all four columns of a row in one
+// 16-byte copy (a column the thread does not own reads whatever the segment
+// buffer holds there and is never flushed; xb + 3 < pitch since pitch is a
+// multiple of 4).
 template <int KY>
 __device__ __forceinline__ void prefetch_lap(const TbParams& p, const Ctx& x, int n) {
   const float* sl = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
                     ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
   float* dst = x.s_lap + (x.w * KY) * RX + 4 * x.lane;
 #pragma unroll
-  for (int r = 0; r < KY; ++r) {
-    if ((x.own_rows >> r) & 1u) {
-      if (x.own_cols == 0xFu) {
-        cp_async16(dst + r * RX, sl + (long long)r * p.pitch);
-      } else {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          if ((x.own_cols >> c) & 1u) cp_async4(dst + r * RX + c, sl + (long long)r * p.pitch + c);
-        }
-      }
-    }
-  }
+  for (int r = 0; r < KY; ++r)
+    if ((x.own_rows >> r) & 1u) cp_async16(dst + r * RX, sl + (long long)r * p.pitch);
   cp_async_commit();
 }
 
