@@ -43,6 +43,7 @@ struct Ctx {
   int rx0, ry0, flags;
   int y0, xb;               // global row of this thread's r = 0, column of c = 0
   unsigned own_rows, own_cols;
+  unsigned rfull, rpart;    // owned band rows of a thread owning all / some of its 4 columns
   unsigned mask, smask;     // band rows holding receiver taps / source nodes
   unsigned rowvalid;        // band rows inside the domain (adjoint coefficient loads)
   int base, sbase;          // first staged tap row / source row of this thread
@@ -140,9 +141,14 @@ __device__ __forceinline__ void prefetch_lap(const TbParams& p, const Ctx& x, in
   const float* sl = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
                     ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
   float* dst = x.s_lap + (x.w * KY) * RX + 4 * x.lane;
+  if (x.own_rows == (1u << KY) - 1u) {  // warp-uniform: a band owned in full
 #pragma unroll
-  for (int r = 0; r < KY; ++r)
-    if ((x.own_rows >> r) & 1u) cp_async16(dst + r * RX, sl + (long long)r * p.pitch);
+    for (int r = 0; r < KY; ++r) cp_async16(dst + r * RX, sl + (long long)r * p.pitch);
+  } else {
+#pragma unroll
+    for (int r = 0; r < KY; ++r)
+      if ((x.own_rows >> r) & 1u) cp_async16(dst + r * RX, sl + (long long)r * p.pitch);
+  }
   cp_async_commit();
 }
 
@@ -347,11 +353,14 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
     float rgt = __shfl_down_sync(FULL, cur.x, 1);
     if (lzero) lft = 0.f;
     if (rzero) rgt = 0.f;
-    // nbr4 / lap5 / leap of fdtd_device.cuh on cell pairs (0,1) and (2,3)
+    // nbr4 / lap5 / leap of fdtd_device.cuh on cell pairs (0,1) and (2,3). The
+    // left + right sums are scalar: their operands (lft, c0), (c1, c2), (c3, rgt)
+    // straddle the register pairs, and a paired add would first need them
+    // copied into place (more instructions than the four scalar adds).
     const float2 udA = __fadd2_rn(make_float2(prv.x, prv.y), make_float2(nxt.x, nxt.y));
     const float2 udB = __fadd2_rn(make_float2(prv.z, prv.w), make_float2(nxt.z, nxt.w));
-    const float2 lrA = __fadd2_rn(make_float2(lft, cur.x), make_float2(cur.y, cur.z));
-    const float2 lrB = __fadd2_rn(make_float2(cur.y, cur.z), make_float2(cur.w, rgt));
+    const float2 lrA = make_float2(__fadd_rn(lft, cur.y), __fadd_rn(cur.x, cur.z));
+    const float2 lrB = make_float2(__fadd_rn(cur.y, cur.w), __fadd_rn(cur.z, rgt));
     const float2 nA = __ffma2_rn(udA, J2, __fmul2_rn(lrA, I2));
     const float2 nB = __ffma2_rn(udB, J2, __fmul2_rn(lrB, I2));
     {
@@ -359,11 +368,13 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
       const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), D2, nA);
       const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), D2, nB);
       const float l0 = lA.x, l1 = lA.y, l2 = lB.x, l3 = lB.y;
-      if (MODE == MODE_REC && ((x.own_rows >> r) & 1u)) {
+      if (MODE == MODE_REC) {
+        // whole owned rows in one 16-byte store; the per-column form only in the
+        // rare warps holding a lane that owns part of its columns
         float* dst = segrow + (long long)r * p.pitch;
-        if (x.own_cols == 0xFu) {
+        if ((x.rfull >> r) & 1u) {
           *reinterpret_cast<float4*>(dst) = make_float4(l0, l1, l2, l3);
-        } else {
+        } else if ((x.rpart >> r) & 1u) {
           if (x.own_cols & 1u) dst[0] = l0;
           if (x.own_cols & 2u) dst[1] = l1;
           if (x.own_cols & 4u) dst[2] = l2;
@@ -591,6 +602,8 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
       const int xx = x.xb + c;
       if (xx >= t.ox0 && xx < t.ox1) x.own_cols |= 1u << c;
     }
+    x.rfull = (x.own_cols == 0xFu) ? x.own_rows : 0u;
+    x.rpart = (x.own_cols != 0xFu && x.own_cols) ? x.own_rows : 0u;
 
     // coefficients of the region (zero outside the domain; the padding columns of
     // coef are zero in memory)
