@@ -38,6 +38,13 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
+// Edge work of one warp for one item (warp-uniform). EK_EDGE is the compact
+// form for the usual placements (row 0 at band row 0, row ny-1 at band row
+// KY-1, column nx-1 not in column 0 of a lane); EK_ALL is the general form.
+// Keeping the per-step loop of every common case small keeps it in the
+// instruction cache.
+constexpr int EK_NONE = 0, EK_EDGE = 1, EK_ALL = 2;
+
 struct Ctx {
   int tid, w, lane, nw, s;
   int rx0, ry0, flags;
@@ -222,6 +229,77 @@ __device__ __forceinline__ void mur_row_at(float (&P)[KY][4], const float (&C)[K
   if constexpr (R + 1 < KY) mur_row_at<KY, WF, DIR, R + 1>(P, C, re, k, ratio, xb, nx);
 }
 
+// Mur row RE of one lane from the inner row RI on all four columns. The cells
+// this also touches besides columns 1 .. nx-2 are corners (overwritten below)
+// and padding columns (k = 0 and zero operands keep them zero).
+template <int KY, bool WF, int RE, int RI>
+__device__ __forceinline__ void mur_row_all(float (&P)[KY][4], const float (&C)[KY][4], const float* k,
+                                            const float* ratio) {
+  const float4 kv = *reinterpret_cast<const float4*>(k);
+  const float4 rv = WF ? *reinterpret_cast<const float4*>(ratio) : make_float4(1.f, 1.f, 1.f, 1.f);
+  P[RE][0] = mur_edge<WF>(rv.x, C[RI][0], kv.x, P[RI][0], C[RE][0]);
+  P[RE][1] = mur_edge<WF>(rv.y, C[RI][1], kv.y, P[RI][1], C[RE][1]);
+  P[RE][2] = mur_edge<WF>(rv.z, C[RI][2], kv.z, P[RI][2], C[RE][2]);
+  P[RE][3] = mur_edge<WF>(rv.w, C[RI][3], kv.w, P[RI][3], C[RE][3]);
+}
+
+// Corner (band row R, lane column CE) as the average of the x-direction Mur from
+// column CI and the y-direction Mur from band row RN; kC[ci] / kC[4 + ci] are the
+// corner's kx / ky (ratios rofs further on for the w-form).
+template <int KY, bool WF, int R, int RN, int CE, int CI>
+__device__ __forceinline__ void corner(float (&P)[KY][4], const float (&C)[KY][4], const float* kC, int ci,
+                                       int rofs) {
+  const float fx = mur_edge<WF>(WF ? kC[rofs + ci] : 1.0f, C[R][CI], kC[ci], P[R][CI], C[R][CE]);
+  const float fy = mur_edge<WF>(WF ? kC[rofs + 4 + ci] : 1.0f, C[RN][CE], kC[4 + ci], P[RN][CE], C[R][CE]);
+  P[R][CE] = corner_avg(fx, fy);
+}
+
+// Right-edge work in lane L1 for the column c1 = 1, 2, 3 holding nx-1 (inner
+// column c1 - 1 in the same lane): the column over every band row, then the
+// corners of the rows the band holds.
+template <int KY, bool WF, int CE>
+__device__ __forceinline__ void right_fast(float (&P)[KY][4], const float (&C)[KY][4], const float* kR,
+                                           const float* kC, int rofs, bool bot, bool top) {
+  mur_column<KY, WF, CE, CE - 1>(P, C, kR, kR + rofs, 0, KY - 1);
+  if (bot) corner<KY, WF, 0, 1, CE, CE - 1>(P, C, kC, 1, rofs);
+  if (top) corner<KY, WF, KY - 1, KY - 2, CE, CE - 1>(P, C, kC, 3, rofs);
+}
+
+// EK_EDGE: Mur rows on whole lane rows, columns on every band row, then the
+// corners, which overwrite the four corner cells the rows and columns also
+// touched (the reference's order: rows and columns from the same field, corners
+// from their updated neighbours).
+template <int KY, bool WF>
+__device__ __forceinline__ void boundary_fast(float (&P)[KY][4], const float (&C)[KY][4],
+                                              const TbParams& p, const Ctx& x) {
+  const int ry = x.nw * KY;
+  const float* kL = x.s_mur;
+  const float* kR = kL + ry;
+  const float* kB = kR + ry;
+  const float* kT = kB + RX;
+  const float* kC = kT + RX;
+  const int rofs = 2 * ry + 2 * RX + 8;
+  const int lr0 = x.w * KY, lc0 = 4 * x.lane;
+  const bool bot = (x.flags & TF_BOTTOM) && x.y0 == 0;                // warp-uniform
+  const bool top = (x.flags & TF_TOP) && x.y0 + KY == p.ny;           // warp-uniform
+  if (bot) mur_row_all<KY, WF, 0, 1>(P, C, kB + lc0, kB + rofs + lc0);
+  if (top) mur_row_all<KY, WF, KY - 1, KY - 2>(P, C, kT + lc0, kT + rofs + lc0);
+  if ((x.flags & TF_LEFT) && x.lane == 0) {
+    mur_column<KY, WF, 0, 1>(P, C, kL + lr0, kL + rofs + lr0, 0, KY - 1);
+    if (bot) corner<KY, WF, 0, 1, 0, 1>(P, C, kC, 0, rofs);
+    if (top) corner<KY, WF, KY - 1, KY - 2, 0, 1>(P, C, kC, 2, rofs);
+  }
+  if (x.flags & TF_RIGHT) {
+    const int lx1 = p.nx - 1 - x.rx0;
+    if (x.lane == (lx1 >> 2)) {
+      const int c1 = lx1 & 3;   // 1, 2 or 3 in this variant
+      if (c1 == 3) right_fast<KY, WF, 3>(P, C, kR + lr0, kC, rofs, bot, top);
+      else if (c1 == 2) right_fast<KY, WF, 2>(P, C, kR + lr0, kC, rofs, bot, top);
+      else right_fast<KY, WF, 1>(P, C, kR + lr0, kC, rofs, bot, top);
+    }
+  }
+}
+
 template <int KY, bool WF>
 __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY][4],
                                          const TbParams& p, const Ctx& x) {
@@ -319,7 +397,7 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
   }
 }
 
-template <int KY, int MODE, bool EDGE>
+template <int KY, int MODE, int EK>
 __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
                                         const TbParams& p, const Ctx& x, int k) {
   const int n = (MODE == MODE_ADJ) ? p.n0 - k : p.n0 + k;
@@ -339,8 +417,8 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   float4 cur = opval(C[0]);
   // Column 0 and column nx-1 are always overwritten by the Mur update, so only
   // the recompute, which stores lap(u) itself, needs the zero outside the domain.
-  const bool lzero = EDGE && MODE == MODE_REC && x.lane == 0 && x.rx0 == 0;
-  const bool rzero = EDGE && MODE == MODE_REC && x.lane == 31 && (x.rx0 + RX >= p.nx);
+  const bool lzero = EK != EK_NONE && MODE == MODE_REC && x.lane == 0 && x.rx0 == 0;
+  const bool rzero = EK != EK_NONE && MODE == MODE_REC && x.lane == 31 && (x.rx0 + RX >= p.nx);
   float* segrow = nullptr;
   if (MODE == MODE_REC) {
     segrow = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
@@ -430,7 +508,8 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
 
   // ---- Mur edges and corners, zero outside the domain
-  if (EDGE) boundary<KY, MODE == MODE_ADJ>(P, C, p, x);
+  if (EK == EK_EDGE) boundary_fast<KY, MODE == MODE_ADJ>(P, C, p, x);
+  if (EK == EK_ALL) boundary<KY, MODE == MODE_ADJ>(P, C, p, x);
 
   // ---- receiver taps (forward) / imaging (adjoint)
   if (MODE == MODE_FWD && x.mask) {
@@ -515,7 +594,7 @@ __device__ __forceinline__ void store_state(const TbParams& p, const Ctx& x,
   }
 }
 
-template <int KY, int MODE, bool EDGE>
+template <int KY, int MODE, int EK>
 __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
   float P[KY][4], C[KY][4];
   const long long sbase = (long long)x.s * p.ny * p.pitch;
@@ -529,7 +608,7 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
     }
     P[r][0] = a.x; P[r][1] = a.y; P[r][2] = a.z; P[r][3] = a.w;
     C[r][0] = b.x; C[r][1] = b.y; C[r][2] = b.z; C[r][3] = b.w;
-    if (EDGE) {
+    if (EK != EK_NONE) {
       // padding columns start at zero whatever the buffer holds there
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
@@ -543,8 +622,8 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
   __syncthreads();
 
   for (int k = 0; k < p.nsteps; k += 2) {
-    substep<KY, MODE, EDGE>(P, C, p, x, k);
-    if (k + 1 < p.nsteps) substep<KY, MODE, EDGE>(C, P, p, x, k + 1);
+    substep<KY, MODE, EK>(P, C, p, x, k);
+    if (k + 1 < p.nsteps) substep<KY, MODE, EK>(C, P, p, x, k + 1);
   }
   if (p.nsteps & 1) {
     store_state<KY>(p, x, C, P);
@@ -724,14 +803,18 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
     // Edge code only in warps with edge cells: every warp of a tile holding the
     // left or right edge (column 0 / nx-1 and the padding columns sit in every
     // band), only the warps holding row 0 or row ny-1 otherwise. Warps of one CTA
-    // may take different variants: both pass the same per-step barriers.
-    const bool warp_edge = (t.flags & (TF_LEFT | TF_RIGHT)) ||
-                           ((t.flags & TF_BOTTOM) && x.y0 <= 0 && x.y0 + KY > 0) ||
-                           ((t.flags & TF_TOP) && x.y0 <= p.ny - 1 && x.y0 + KY > p.ny - 1);
-    if (warp_edge) {
-      run_item<KY, MODE, true>(p, x);
+    // may take different variants: all pass the same per-step barriers.
+    const bool row_b = (t.flags & TF_BOTTOM) && x.y0 <= 0 && x.y0 + KY > 0;
+    const bool row_t = (t.flags & TF_TOP) && x.y0 <= p.ny - 1 && x.y0 + KY > p.ny - 1;
+    const bool cols = t.flags & (TF_LEFT | TF_RIGHT);
+    const bool fast = (!row_b || x.y0 == 0) && (!row_t || x.y0 + KY == p.ny) && !(row_b && row_t) &&
+                      (!(t.flags & TF_RIGHT) || ((p.nx - 1 - t.rx0) & 3) != 0);
+    if (!row_b && !row_t && !cols) {
+      run_item<KY, MODE, EK_NONE>(p, x);
+    } else if (fast) {
+      run_item<KY, MODE, EK_EDGE>(p, x);
     } else {
-      run_item<KY, MODE, false>(p, x);
+      run_item<KY, MODE, EK_ALL>(p, x);
     }
 
     if (MODE == MODE_FWD) {
