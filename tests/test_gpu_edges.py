@@ -1,10 +1,10 @@
 """Sources and receivers in the lanes holding the Mur edges.
 
-The temporally blocked kernel updates the Mur columns inside its stencil loop
-when no injection node (a source, or in the adjoint a receiver tap) sits in the
-4-column lane group holding column 0 or nx-1; otherwise that warp takes the
-general edge path. Both must equal the plain per-step engine: the forward bit
-for bit, the gradient to the float64 summation order.
+Injection nodes (sources; in the adjoint, receiver taps) on and beside column
+0, column nx-1 and the edge rows, for the three positions of column nx-1 inside
+a lane's 4-column group that select the kernel's compact or general edge path.
+Both must equal the plain per-step engine: the forward bit for bit, the
+gradient to the float64 summation order.
 """
 
 import numpy as np
