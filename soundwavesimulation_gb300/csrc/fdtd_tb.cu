@@ -594,9 +594,11 @@ __device__ __forceinline__ void store_state(const TbParams& p, const Ctx& x,
   }
 }
 
-template <int KY, int MODE, int EK>
-__device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
-  float P[KY][4], C[KY][4];
+// The item's two state fields, this thread's band rows (zero outside the domain;
+// padding columns start at zero whatever the buffer holds there). Issued at the
+// start of the item so that their latency overlaps the table setup.
+template <int KY>
+__device__ __forceinline__ void load_state(const TbParams& p, const Ctx& x, float (&P)[KY][4], float (&C)[KY][4]) {
   const long long sbase = (long long)x.s * p.ny * p.pitch;
 #pragma unroll
   for (int r = 0; r < KY; ++r) {
@@ -608,14 +610,36 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x) {
     }
     P[r][0] = a.x; P[r][1] = a.y; P[r][2] = a.z; P[r][3] = a.w;
     C[r][0] = b.x; C[r][1] = b.y; C[r][2] = b.z; C[r][3] = b.w;
-    if (EK != EK_NONE) {
-      // padding columns start at zero whatever the buffer holds there
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        if (x.xb + c >= p.nx) { P[r][c] = 0.f; C[r][c] = 0.f; }
-      }
+    for (int c = 0; c < 4; ++c) {
+      if (x.xb + c >= p.nx) { P[r][c] = 0.f; C[r][c] = 0.f; }
     }
   }
+}
+
+// Pulls the state rows of this thread in item `item` (the CTA's next one) into
+// L2 while the current item computes.
+template <int KY>
+__device__ __forceinline__ void prefetch_state(const TbParams& p, const Ctx& x, int item) {
+  const int ti = item / p.nshots;
+  const int s = item - ti * p.nshots;
+  const TbTile& t = p.tiles[ti];
+  const int y0 = t.ry0 + x.w * KY, xb = t.rx0 + 4 * x.lane;
+  if (xb >= p.pitch) return;
+  const long long sbase = (long long)s * p.ny * p.pitch;
+#pragma unroll
+  for (int r = 0; r < KY; ++r) {
+    const int yy = y0 + r;
+    if (yy >= 0 && yy < p.ny) {
+      const long long o = sbase + (long long)yy * p.pitch + xb;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(p.in_prev + o));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(p.in_cur + o));
+    }
+  }
+}
+
+template <int KY, int MODE, int EK>
+__device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x, float (&P)[KY][4], float (&C)[KY][4]) {
   x.s_xch[x.w * 64 + x.lane] = opval(C[0]);
   x.s_xch[x.w * 64 + 32 + x.lane] = opval(C[KY - 1]);
   if (MODE == MODE_ADJ && x.own_rows && x.own_cols && p.n0 >= 1) prefetch_lap<KY>(p, x, p.n0);
@@ -645,9 +669,10 @@ __device__ __forceinline__ void bind_ctx(const TbParams& p, Ctx& x, unsigned cha
   x.s_src = reinterpret_cast<float*>(smem + L.src);
 }
 
-// One (tile, shot) item: load, T steps, store, traces / gradient flush.
+// One (tile, shot) item: load, T steps, store, traces / gradient flush; `next` is
+// the CTA's next item of the same launch (or -1), whose state is prefetched.
 template <int KY, int MODE>
-__device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char* smem, int item) {
+__device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char* smem, int item, int next) {
   const int nw = p.nwarps;
   const int nthr = nw * 32;
   const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef, p.nsrow_max);
@@ -683,6 +708,9 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
     }
     x.rfull = (x.own_cols == 0xFu) ? x.own_rows : 0u;
     x.rpart = (x.own_cols != 0xFu && x.own_cols) ? x.own_rows : 0u;
+    float P[KY][4], C[KY][4];
+    load_state<KY>(p, x, P, C);
+    if (next >= 0) prefetch_state<KY>(p, x, next);
 
     // coefficients of the region (zero outside the domain; the padding columns of
     // coef are zero in memory)
@@ -810,11 +838,11 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
     const bool fast = (!row_b || x.y0 == 0) && (!row_t || x.y0 + KY == p.ny) && !(row_b && row_t) &&
                       (!(t.flags & TF_RIGHT) || ((p.nx - 1 - t.rx0) & 3) != 0);
     if (!row_b && !row_t && !cols) {
-      run_item<KY, MODE, EK_NONE>(p, x);
+      run_item<KY, MODE, EK_NONE>(p, x, P, C);
     } else if (fast) {
-      run_item<KY, MODE, EK_EDGE>(p, x);
+      run_item<KY, MODE, EK_EDGE>(p, x, P, C);
     } else {
-      run_item<KY, MODE, EK_ALL>(p, x);
+      run_item<KY, MODE, EK_ALL>(p, x, P, C);
     }
 
     if (MODE == MODE_FWD) {
@@ -896,7 +924,8 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   // Items are (tile, shot) pairs with shots varying fastest, dealt out with a
   // grid stride: at any moment the CTAs hold a mix of edge, interior and
   // receiver-heavy tiles, which balances better than contiguous runs per CTA.
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x) run_one<KY, MODE>(p, x, smem, item);
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x)
+    run_one<KY, MODE>(p, x, smem, item, item + (int)gridDim.x < nitems ? item + (int)gridDim.x : -1);
   tm_end<MODE>(x, tm_base);
 }
 
@@ -926,7 +955,7 @@ __global__ void __launch_bounds__(MAXT, 1) tb_group_kernel(const TbGroup g) {
       bind_ctx<KY, MODE>(sp, x, smem);
       cur = pi;
     }
-    run_one<KY, MODE>(sp, x, smem, item - __ldg(g.item_off + pi));
+    run_one<KY, MODE>(sp, x, smem, item - __ldg(g.item_off + pi), -1);
   }
   tm_end<MODE>(x, tm_base);
 }
