@@ -23,8 +23,13 @@
 //     receiver taps and source nodes as per-step shared-memory stages of whole
 //     4-cell rows, Mur coefficients from a per-tile shared-memory table, the
 //     adjoint's gradient tile in tensor memory (tcgen05) and its Laplacian
-//     stream one step ahead through cp.async.
-// The stencil runs on cell pairs with the two-lane float32 instructions; like
+//     stream one step ahead through cp.async;
+//   - each warp runs one of three loop variants per item: no edge work, the
+//     compact edge form (edge rows at fixed band rows, whole-row Mur updates,
+//     corners last) or the general one; the per-step loop of the common cases
+//     stays small, which keeps it in the instruction cache.
+// The stencil runs on cell pairs with the two-lane float32 instructions (the
+// x-neighbour sums, whose operands straddle register pairs, are scalar); like
 // the scalar helpers in fdtd_device.cuh every element is one IEEE
 // round-to-nearest operation, so the values are bit-identical to the one-step
 // kernels in fdtd_kernels.cu. `tb_group_kernel` runs the items of several plans
