@@ -37,7 +37,7 @@ GRAD_BYTES_PER_CELL = 28.0   # forward 12 + adjoint 12 + one read of the forward
 # DRAM bytes (read + write) of one forward launch at 512^2 x 128 shots, by launch shape
 # (rows per lane, warps, steps per launch), from one ncu capture of that launch
 # (profiles/tb_kernel_fwd_512x512x128.md)
-FWD_TRAFFIC = {(8, 16, 15): 329.325824e6 + 228.232704e6}
+FWD_TRAFFIC = {(8, 16, 15): 335.443712e6 + 228.196864e6}
 
 
 def peaks():
