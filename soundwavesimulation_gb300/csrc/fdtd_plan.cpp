@@ -73,6 +73,14 @@ std::string tile_axis(int n, int region, int align, int halo, int band, std::vec
       origin -= (align > 1 ? align : 1);
       if (++tries > 64) return "no region placement satisfies the band constraint";
     }
+    if (band > 1 && origin > 0 && origin + region >= n) {
+      // the last region: move it down (more overlap) until row n-1 is the last
+      // row of its band, if it still reaches n, so that the kernel's compact edge
+      // loop applies to the band holding row n-1
+      int o = origin;
+      while (o > 0 && (n - 1 - o) % band != band - 1) o -= (align > 1 ? align : 1);
+      if (o > 0 && o + region >= n && band_ok(n, o, region, band)) origin = o;
+    }
     const int end = origin + region;
     int own1 = (end >= n) ? n : end - halo;
     if (origin > 0 && own0 < origin + halo) return "tiler produced an unsafe low border";

@@ -121,6 +121,21 @@ def test_tiler_invariants(n, region, align, halo, band):
                 assert (n - 1 - origin) % band != 0
 
 
+@pytest.mark.parametrize("n", [256, 384, 512, 1024])
+@pytest.mark.parametrize("band,halo", [(8, 16), (4, 16), (8, 11)])
+def test_config_grids_take_the_compact_edge_path(n, band, halo):
+    """At the configuration grid sizes the tiler puts row 0 at band row 0, row n-1
+    at band row `band` - 1 and column n-1 at column 3 of a lane: the placements
+    for which the temporally blocked kernel runs its compact edge loop."""
+    from soundwavesimulation_gb300 import _lib
+    ty = _lib.tile_axis(n, 128, 1, halo, band)
+    assert ty[0, 0] == 0
+    last = int(ty[-1, 0])
+    assert (n - 1 - last) % band == band - 1
+    tx = _lib.tile_axis(n, 128, 4, halo, 0)
+    assert (n - 1 - int(tx[-1, 0])) % 4 == 3
+
+
 def test_tap_table_sums_every_receiver_weight():
     from soundwavesimulation_gb300 import RingArray, axis_centers, _lib
     ax = axis_centers(41, 2e-3)
