@@ -2,7 +2,7 @@
 
 The oracle (float64 NumPy restatement of the reference, pinned to the
 reference's own outputs in test_oracle_golden.py) is the checker. Tolerances:
-traces rel-L2 <= 1e-5 against float64 (the spec trace budget), one-step
+traces rel-L2 <= 1e-5 against float64 (the required trace budget), one-step
 kernels <= 1e-6; the fused engine and the one-step kernels run the same
 float32 arithmetic and must agree bit for bit.
 """

@@ -1,6 +1,6 @@
 """GPU parity of the FWI gradient: fused checkpointed adjoint vs the reference and the oracle.
 
-Tolerances: gradient rel-L2 <= 1e-3 against float64 (the spec budget; the
+Tolerances: gradient rel-L2 <= 1e-3 against float64 (the required budget; the
 float32 engine lands near 1e-5), misfit rel 1e-5. The checkpointed gradient must
 not depend on the checkpoint spacing beyond float32 summation order, and 16-bit
 checkpoints must stay within 1e-3 of float32 storage.
