@@ -34,10 +34,21 @@ METRIC = "Gcell-updates/s fwd & FWI grad at 512²×128 shots; % HBM peak; vs pla
 UNIT = "Gcell-updates/s"
 FWD_BYTES_PER_CELL = 12.0    # read u, read u_old, write u_next (float32)
 GRAD_BYTES_PER_CELL = 28.0   # forward 12 + adjoint 12 + one read of the forward field 4
-# DRAM bytes (read + write) of one forward launch at 512^2 x 128 shots, by launch shape
-# (rows per lane, warps, steps per launch), from one ncu capture of that launch
-# (profiles/tb_kernel_fwd_512x512x128.md)
-FWD_TRAFFIC = {(8, 16, 15): 335.443712e6 + 228.196864e6}
+# DRAM bytes (read + write) of one forward launch at 512^2 x 128 shots, from one ncu
+# capture of that launch, keyed by the digest of the kernel sources it was taken on
+# and the launch shape (rows per lane, warps, steps per launch). A bench run on
+# other sources or another shape reports the figure as null.
+FWD_TRAFFIC = {("3f0b5a6e9ed8", 8, 16, 15): 335.443712e6 + 228.196864e6}
+KERNEL_SOURCES = ("soundwavesimulation_gb300/csrc/fdtd_tb.cu", "soundwavesimulation_gb300/csrc/fdtd_device.cuh")
+
+
+def kernel_digest():
+    """First 12 hex digits of the SHA-256 of the temporally blocked kernel's sources."""
+    import hashlib
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        h.update((ROOT / rel).read_bytes())
+    return h.hexdigest()[:12]
 
 
 def peaks():
@@ -397,8 +408,12 @@ def run_ours(args):
     hbm, peak_kind = peaks()
     achieved = FWD_BYTES_PER_CELL * acq.cell_updates / (ms * 1e-3) / 1e9
     launch_us = ms * 1e3 / launches_per_pass
-    shape = (plan.tuning["rows_per_lane"], plan.tuning["warps"], plan.tuning["steps_per_launch"])
+    digest = kernel_digest()
+    shape = (digest, plan.tuning["rows_per_lane"], plan.tuning["warps"], plan.tuning["steps_per_launch"])
     traffic = FWD_TRAFFIC.get(shape) if (n, S) == (512, 128) else None
+    # compulsory DRAM bytes of one launch: u_old and u read and written once per cell
+    # (16 B per cell and shot) plus the launch's trace samples
+    compulsory = 16.0 * n * n * S + 4.0 * acq.n_elements * S * plan.tuning["steps_per_launch"]
     out = None
     if rank == 0:
         workers = cpu_workers()
@@ -416,10 +431,13 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "launch_us": launch_us,
                          "dram_frac": (traffic / (launch_us * 1e-6) / 1e9 / hbm) if traffic else None,
+                         "compulsory_bytes": compulsory, "kernel_digest": digest,
                          "note": f"12 B per cell-update algorithmic; peak {peak_kind}; temporal blocking "
                                  "makes the algorithmic fraction exceed the single-step roofline; traffic = "
-                                 "ncu dram bytes read+written per launch for this launch shape "
-                                 "(profiles/tb_kernel_fwd_512x512x128.md), dram_frac = traffic / launch_us / peak"},
+                                 "ncu dram bytes read+written per launch, taken on the kernel sources of "
+                                 "kernel_digest at this launch shape (null otherwise); dram_frac = traffic / "
+                                 "launch_us / peak; compulsory_bytes = one read and one write of both state "
+                                 "fields plus the launch's traces"},
             "plain": {"value": plain_value, "unit": UNIT, "shots_sampled": plain_shots,
                       "speedup": value / world / plain_value, "bitwise_equal_traces": same},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

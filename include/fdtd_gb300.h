@@ -260,11 +260,16 @@ size_t fdtd_gradient_plain_workspace(const fdtd_problem* problem);
    fdtd_forward_plain, no workspace: the scratch is a file-scope device array of
    FDTD_STATIC_SCRATCH_BYTES that every GPU loading the library holds until exit.
    Calls no cudaMalloc, cudaFree or allocating library routine. Problems that do
-   not fit return FDTD_ERR_WORKSPACE with a message. The first call on a device
-   looks up the array's address (cudaGetSymbolAddress, that device current) and
-   caches it: make that first call before any stream capture. All calls share
-   the array and it keeps the last call's contents (each shot clears the fields
-   it uses); calls that overlap on the GPU race on it. */
+   not fit return FDTD_ERR_WORKSPACE with a message; bad receivers, source
+   nodes or waveform indices return FDTD_ERR_INVALID before any device work. The
+   first call on a device looks up the array's address (cudaGetSymbolAddress,
+   that device current) and caches it: make that first call before any stream
+   capture. The cached address belongs to the device's primary context; a
+   cudaDeviceReset or a non-primary context is not supported. Every call copies
+   the receiver and source tables from the host arrays into the array and
+   synchronises `stream` before the time loop. All calls share the array and it
+   keeps the last call's contents (each shot clears the fields it uses); calls
+   that overlap on the GPU race on it. */
 int32_t fdtd_forward_plain_static(const fdtd_problem* problem, float* traces, void* stream);
 
 /* ------------------------------------------------------- tiling (host) */

@@ -420,3 +420,92 @@ def resize_slowness(m, source_axes, target_axes, background_m):
         out = out + row * wy[r]
     out[(np.abs(uu) > 1.0) | (np.abs(vv) > 1.0)] = background_m
     return out
+
+
+# ---------------------------------------------------------------------------
+# Regularisers and projected Adam (fdtd2d/inversion/misfit.py, invert_ring.py)
+# ---------------------------------------------------------------------------
+
+def _mask_pairs(mask, axis):
+    """Forward-difference pairs along ``axis`` whose two pixels are both inside."""
+    if axis == 1:
+        return mask[:, 1:] & mask[:, :-1]
+    return mask[1:, :] & mask[:-1, :]
+
+
+def tikhonov(m, mask, alpha):
+    """Value and gradient of 0.5 * alpha * sum of squared in-mask forward differences.
+
+    Restates fdtd2d/inversion/misfit.py:19-44: a difference counts only when
+    both its pixels lie in the mask; the gradient is zero outside the mask.
+    """
+    m = np.asarray(m, dtype=float)
+    mask = np.asarray(mask, dtype=bool)
+    grad = np.zeros_like(m)
+    if alpha <= 0.0:
+        return 0.0, grad
+    total = 0.0
+    for axis in (1, 0):
+        pairs = _mask_pairs(mask, axis)
+        diff = np.diff(m, axis=axis)
+        total += 0.5 * alpha * float(np.sum(diff[pairs] ** 2))
+        flux = np.where(pairs, alpha * diff, 0.0)
+        hi = (slice(None), slice(1, None)) if axis == 1 else (slice(1, None), slice(None))
+        lo = (slice(None), slice(None, -1)) if axis == 1 else (slice(None, -1), slice(None))
+        grad[hi] += flux
+        grad[lo] -= flux
+    grad[~mask] = 0.0
+    return total, grad
+
+
+def total_variation(m, mask, alpha, eps):
+    """Value and gradient of alpha * sum(sqrt(|grad m|^2 + eps^2) - eps).
+
+    Restates fdtd2d/inversion/misfit.py:47-71: in-mask forward differences
+    (zero where a pair leaves the mask, and in the last row / column), the
+    smoothed norm per pixel, and the gradient zeroed outside the mask.
+    """
+    m = np.asarray(m, dtype=float)
+    mask = np.asarray(mask, dtype=bool)
+    grad = np.zeros_like(m)
+    if alpha <= 0.0:
+        return 0.0, grad
+    ddx = np.zeros_like(m)
+    ddy = np.zeros_like(m)
+    ddx[:, :-1] = np.where(_mask_pairs(mask, 1), np.diff(m, axis=1), 0.0)
+    ddy[:-1, :] = np.where(_mask_pairs(mask, 0), np.diff(m, axis=0), 0.0)
+    norm = np.sqrt(ddx * ddx + ddy * ddy + eps * eps)
+    value = alpha * float(np.sum(norm - eps))
+    qx = alpha * ddx / norm
+    qy = alpha * ddy / norm
+    grad -= qx + qy
+    grad[:, 1:] += qx[:, :-1]
+    grad[1:, :] += qy[:-1, :]
+    grad[~mask] = 0.0
+    return value, grad
+
+
+def projected_adam(m0, misfit_and_grad, project, mask, learning_rate, iterations,
+                   beta1=0.9, beta2=0.999, epsilon=1e-30):
+    """The iterates of projected Adam (invert_ring.py:817-861).
+
+    Moments update on the mask only; the bias-corrected step
+    ``lr * m_hat / (sqrt(v_hat) + eps)`` is applied on the mask and the result
+    projected. Returns the model after each of ``iterations`` steps.
+    """
+    mask = np.asarray(mask, dtype=bool)
+    m = project(np.asarray(m0, dtype=float))
+    _, g = misfit_and_grad(m)
+    first = np.zeros_like(m)
+    second = np.zeros_like(m)
+    out = []
+    for k in range(1, iterations + 1):
+        first[mask] = beta1 * first[mask] + (1.0 - beta1) * g[mask]
+        second[mask] = beta2 * second[mask] + (1.0 - beta2) * g[mask] ** 2
+        step = np.zeros_like(m)
+        step[mask] = learning_rate * (first[mask] / (1.0 - beta1 ** k)) / (
+            np.sqrt(second[mask] / (1.0 - beta2 ** k)) + epsilon)
+        m = project(m - step)
+        _, g = misfit_and_grad(m)
+        out.append(m.copy())
+    return out

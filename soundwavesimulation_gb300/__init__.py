@@ -7,12 +7,12 @@ and function names, backed by hand-written CUDA kernels in ``libfdtd_gb300.so``
 """
 
 from .geometry import ArcArray, RingArray, axis_centers, n_steps_for_crossing, stable_dt
-from .medium import (c_from_m, clip_m, interior_mask, m_from_c, mute_transmitter, tikhonov,
-                     total_variation, waveform_misfit)
+from .medium import (c_from_m, clip_m, interior_mask, m_from_c, mute_transmitter, regularizers,
+                     tikhonov, total_variation, waveform_misfit)
 from .waveforms import linear_chirp, ricker
 
 __all__ = [
     "ArcArray", "RingArray", "axis_centers", "n_steps_for_crossing", "stable_dt",
-    "c_from_m", "clip_m", "interior_mask", "m_from_c", "mute_transmitter", "tikhonov",
+    "c_from_m", "clip_m", "interior_mask", "m_from_c", "mute_transmitter", "regularizers", "tikhonov",
     "total_variation", "waveform_misfit", "linear_chirp", "ricker",
 ]

@@ -6,6 +6,7 @@
 
 #include <string>
 
+#include "../../include/fdtd_gb300.h"
 #include "fdtd_device.cuh"
 
 namespace fdtd {
@@ -14,6 +15,13 @@ namespace fdtd {
 void set_error(const std::string& msg);
 int32_t fail(int32_t code, const std::string& msg);
 int32_t cuda_fail(cudaError_t e, const char* what);
+
+// Argument checks shared by the entry points (fdtd_plan.cpp): the grid's shape,
+// spacings and medium pointers; for the plain per-shot forms also shots, steps,
+// receivers inside the grid (their 2 x 2 footprint included) and every used
+// source entry's node and waveform index.
+int32_t validate_grid(const fdtd_grid& g);
+int32_t validate_plain_problem(const fdtd_problem& prob);
 
 // Temporally blocked kernel (fdtd_tb.cu).
 cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st);

@@ -15,10 +15,14 @@
 // memory that every GPU loading this library holds until the process exits. On
 // its first call on a device (with that device current) the entry point looks up
 // the array's device address once with cudaGetSymbolAddress and caches it; make
-// that first call before any stream capture. All calls share the array and it
-// keeps the last call's contents, so every field it uses is cleared at the start
-// of each shot; calls that overlap on the GPU (other streams, other threads)
-// race on the array.
+// that first call before any stream capture. The cached address belongs to the
+// device's primary context: a cudaDeviceReset, or a caller that runs in another
+// context of the same device, is not supported. Every call copies the receiver
+// and source tables from the caller's host arrays into the array and then
+// synchronises `stream` before it launches the time loop. All calls share the
+// array and it keeps the last call's contents, so every field it uses is cleared
+// at the start of each shot; calls that overlap on the GPU (other streams, other
+// threads) race on the array.
 
 #include <mutex>
 
@@ -43,19 +47,13 @@ using namespace fdtd;
 
 extern "C" int32_t fdtd_forward_plain_static(const fdtd_problem* prob, float* traces, void* stream) {
   if (!prob || !traces) return fail(FDTD_ERR_INVALID, "null argument");
+  // the same checks as fdtd_forward_plain: grid, spacings, receivers and every
+  // used source entry (node inside the grid, waveform index below n_waves)
+  const int32_t bad = validate_plain_problem(*prob);
+  if (bad) return bad;
   const fdtd_grid& g = prob->grid;
-  if (g.ny < 8 || g.nx < 8 || g.pitch < g.nx || g.pitch % 4) return fail(FDTD_ERR_INVALID, "bad grid shape");
-  if (!g.coef || !g.mur) return fail(FDTD_ERR_INVALID, "coef and mur must be set");
   const int R = prob->rx.n, S = prob->n_shots, nt = prob->n_steps;
-  const int K = prob->src.per_shot > 0 ? prob->src.per_shot : 0;
-  if (R < 1 || S < 1 || nt < 1 || !prob->rx.row0 || !prob->rx.col0 || !prob->rx.w)
-    return fail(FDTD_ERR_INVALID, "receivers, shots and steps must be set");
-  if (K > 0 && (!prob->src.row || !prob->src.col || !prob->src.w || !prob->src.wave || !prob->src.waveforms))
-    return fail(FDTD_ERR_INVALID, "source arrays missing");
-  for (int r = 0; r < R; ++r) {
-    if (prob->rx.row0[r] < 0 || prob->rx.row0[r] > g.ny - 2 || prob->rx.col0[r] < 0 || prob->rx.col0[r] > g.nx - 2)
-      return fail(FDTD_ERR_INVALID, "receiver outside the grid");
-  }
+  const int K = prob->src.per_shot;
   const size_t plane = (size_t)g.ny * g.pitch;
   const size_t off_rc = round256(3 * plane * sizeof(float));
   const size_t off_w = off_rc + round256((size_t)R * 2 * sizeof(int32_t));

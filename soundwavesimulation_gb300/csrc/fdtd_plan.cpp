@@ -154,15 +154,44 @@ struct fdtd_plan {
   }
 };
 
-namespace {
-
-int32_t validate_grid(const fdtd_grid& g) {
+int32_t fdtd::validate_grid(const fdtd_grid& g) {
   if (g.ny < 8 || g.nx < 8) return fail(FDTD_ERR_INVALID, "grid must be at least 8 x 8");
   if (g.pitch < g.nx || g.pitch % 4 != 0) return fail(FDTD_ERR_INVALID, "pitch must be a multiple of 4 and >= nx");
   if (!(g.dx > 0) || !(g.dy > 0) || !(g.dt > 0)) return fail(FDTD_ERR_INVALID, "dx, dy and dt must be positive");
   if (!g.coef || !g.mur) return fail(FDTD_ERR_INVALID, "coef and mur must be set");
   return FDTD_OK;
 }
+
+int32_t fdtd::validate_plain_problem(const fdtd_problem& prob) {
+  int32_t rc = validate_grid(prob.grid);
+  if (rc) return rc;
+  const fdtd_grid& g = prob.grid;
+  if (prob.n_shots < 1 || prob.n_steps < 1) return fail(FDTD_ERR_INVALID, "n_shots and n_steps must be positive");
+  const int R = prob.rx.n;
+  if (R < 1 || !prob.rx.row0 || !prob.rx.col0 || !prob.rx.w) return fail(FDTD_ERR_INVALID, "receivers missing");
+  for (int r = 0; r < R; ++r) {
+    // a receiver samples rows row0, row0 + 1 and columns col0, col0 + 1
+    if (prob.rx.row0[r] < 0 || prob.rx.row0[r] > g.ny - 2 || prob.rx.col0[r] < 0 || prob.rx.col0[r] > g.nx - 2)
+      return fail(FDTD_ERR_INVALID, "receiver " + std::to_string(r) + " lies outside the grid");
+  }
+  const fdtd_sources& src = prob.src;
+  if (src.per_shot < 0) return fail(FDTD_ERR_INVALID, "sources per shot must not be negative");
+  if (src.per_shot == 0) return FDTD_OK;
+  if (!src.row || !src.col || !src.w || !src.wave || !src.waveforms)
+    return fail(FDTD_ERR_INVALID, "source arrays missing");
+  if (src.n_waves < 1 || src.waveform_len < 0) return fail(FDTD_ERR_INVALID, "bad waveform table shape");
+  const size_t n = (size_t)prob.n_shots * src.per_shot;
+  for (size_t e = 0; e < n; ++e) {
+    if (src.wave[e] < 0) continue;  // unused entry
+    if (src.wave[e] >= src.n_waves)
+      return fail(FDTD_ERR_INVALID, "source entry " + std::to_string(e) + ": waveform index out of range");
+    if (src.row[e] < 0 || src.row[e] >= g.ny || src.col[e] < 0 || src.col[e] >= g.nx)
+      return fail(FDTD_ERR_INVALID, "source entry " + std::to_string(e) + " lies outside the grid");
+  }
+  return FDTD_OK;
+}
+
+namespace {
 
 void fill_params(const fdtd_plan* p, TbParams& q) {
   std::memset(&q, 0, sizeof(q));
@@ -1220,7 +1249,7 @@ size_t fdtd_forward_plain_workspace(const fdtd_problem* prob) {
 int32_t fdtd_forward_plain(const fdtd_problem* prob, float* traces, void* workspace, size_t bytes,
                            void* stream) {
   if (!prob || !traces) return fail(FDTD_ERR_INVALID, "null argument");
-  int32_t rc = validate_grid(prob->grid);
+  int32_t rc = validate_plain_problem(*prob);
   if (rc) return rc;
   if (!workspace || bytes < fdtd_forward_plain_workspace(prob)) return fail(FDTD_ERR_WORKSPACE, "workspace too small");
   cudaStream_t st = (cudaStream_t)stream;
@@ -1281,7 +1310,7 @@ int32_t fdtd_gradient_plain(const fdtd_problem* prob, const float* observed, con
                             double* misfit, double* grad_c2, void* workspace, size_t bytes,
                             void* stream) {
   if (!prob || !observed || !misfit || !grad_c2) return fail(FDTD_ERR_INVALID, "null argument");
-  int32_t rc = validate_grid(prob->grid);
+  int32_t rc = validate_plain_problem(*prob);
   if (rc) return rc;
   if (!workspace || bytes < fdtd_gradient_plain_workspace(prob)) return fail(FDTD_ERR_WORKSPACE, "workspace too small");
   cudaStream_t st = (cudaStream_t)stream;

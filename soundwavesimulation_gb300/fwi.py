@@ -27,7 +27,7 @@ import torch
 
 from . import _lib
 from .engine import FusedPlan, chain_rule, residual_misfit
-from .medium import c_from_m, m_from_c, tikhonov, total_variation
+from .medium import c_from_m, m_from_c, regularizers
 from .optim import project_device, regularization_device
 from .torch_backend import TorchFDTD2DBatch, auto_batch_size, engine_tuning
 
@@ -228,9 +228,11 @@ class TorchLeastSquaresFWI:
 
     # --- objective --------------------------------------------------------------
     def regularization(self, m):
-        value, gradient = tikhonov(m, self.mask, self.alpha)
-        tv_value, tv_gradient = total_variation(m, self.mask, self.tv, self.tv_eps)
-        return value + tv_value, gradient + tv_gradient
+        """Tikhonov + total-variation value and gradient of m (float64, host arrays),
+        evaluated by the device kernel (invert_ring.py:662-666)."""
+        if self.alpha <= 0.0 and self.tv <= 0.0:
+            return 0.0, np.zeros(np.shape(m))
+        return regularizers(m, self.mask, self.alpha, self.tv, self.tv_eps, device=self.model.device)
 
     def misfit(self, m):
         """Forward-only J(m) (invert_ring.py:611-632)."""

@@ -1,94 +1,86 @@
-"""Slowness-squared parameterisation, interior mask and host regularisers.
+"""Slowness-squared variable, the interior mask and the regularisers.
 
-Same functions and conventions as the reference's fdtd2d/inversion/medium.py
-and the regularisers of fdtd2d/inversion/misfit.py: the inversion variable is
-m = 1 / c^2; only pixels inside ``radius - margin`` are free.
+The inversion works on m = 1 / c^2 and frees only the pixels strictly inside
+``radius - margin`` of the ring centre; the functions keep the names and
+argument meaning of the reference's fdtd2d/inversion/medium.py and
+fdtd2d/inversion/misfit.py, so a caller can swap the import.
+
+``tikhonov`` and ``total_variation`` evaluate on the GPU through the engine
+library's ``fdtd_regularization`` kernel (float64, NumPy's operation order per
+element); they take and return NumPy arrays like the reference's host versions.
+There is no CPU path: without a CUDA device they raise.
 """
 
 from __future__ import annotations
 
 import numpy as np
+import torch
 
 
 def m_from_c(c):
-    c = np.asarray(c, dtype=float)
-    return 1.0 / (c * c)
+    """Slowness squared of a sound-speed map."""
+    return np.reciprocal(np.square(np.asarray(c, dtype=float)))
 
 
 def c_from_m(m):
-    return 1.0 / np.sqrt(np.asarray(m, dtype=float))
+    """Sound speed of a slowness-squared map."""
+    return np.reciprocal(np.sqrt(np.asarray(m, dtype=float)))
 
 
 def clip_m(m, c_min, c_max):
-    """Clip m so that c stays within [c_min, c_max]."""
-    return np.clip(m, 1.0 / float(c_max) ** 2, 1.0 / float(c_min) ** 2)
+    """m limited to the slowness-squared interval of speeds [c_min, c_max]."""
+    lo, hi = m_from_c(float(c_max)), m_from_c(float(c_min))
+    return np.minimum(np.maximum(m, lo), hi)
 
 
 def interior_mask(x_m, y_m, radius_m, margin_m, center=(0.0, 0.0)):
-    """True where (x, y) lies strictly inside radius - margin."""
-    r = float(radius_m) - float(margin_m)
-    if r <= 0.0:
+    """Boolean (ny, nx) map of the pixels closer than ``radius - margin`` to ``center``."""
+    inner = float(radius_m) - float(margin_m)
+    if inner <= 0.0:
         raise ValueError("Interior radius must be positive; reduce the margin.")
-    x, y = np.meshgrid(np.asarray(x_m, float) - center[0], np.asarray(y_m, float) - center[1],
-                       indexing="xy")
-    return x * x + y * y < r * r
+    ry = np.square(np.asarray(y_m, dtype=float) - float(center[1]))
+    rx = np.square(np.asarray(x_m, dtype=float) - float(center[0]))
+    return np.add.outer(ry, rx) < inner * inner
 
 
 def mute_transmitter(traces, tx):
-    """Copy of the traces with the transmitter channel zeroed."""
-    out = np.array(traces, dtype=float, copy=True)
+    """Float64 copy of a gather (receivers first) with channel ``tx`` set to zero."""
+    out = np.array(traces, dtype=float)
     out[tx] = 0.0
     return out
 
 
 def waveform_misfit(predicted, observed, tx):
-    """0.5 * ||P u - d||^2 without the transmitter channel."""
-    r = mute_transmitter(np.asarray(predicted) - np.asarray(observed), tx)
-    return 0.5 * float(np.sum(r * r))
+    """Half the squared residual norm of one gather, channel ``tx`` left out."""
+    r = mute_transmitter(np.subtract(predicted, observed, dtype=float), tx)
+    return 0.5 * float(np.vdot(r, r))
+
+
+def regularizers(m, mask, alpha, tv, tv_eps, device="cuda"):
+    """Tikhonov (weight ``alpha``) plus total variation (weight ``tv``) of m: the
+    summed value and gradient, zero outside the mask, in one call on ``device``."""
+    from .engine import require_cuda
+    from .optim import regularization_device
+    dev = require_cuda(device)
+    m_d = torch.as_tensor(np.ascontiguousarray(m, dtype=float), device=dev)
+    mask_d = torch.as_tensor(np.ascontiguousarray(mask, dtype=bool), device=dev).to(torch.uint8)
+    grad = torch.zeros_like(m_d)
+    value = torch.zeros(1, dtype=torch.float64, device=dev)
+    regularization_device(m_d, mask_d, alpha, tv, tv_eps, grad, value)
+    return float(value.item()), grad.cpu().numpy()
 
 
 def tikhonov(m, mask, alpha):
-    """0.5 * alpha * sum of squared forward differences inside the mask, and its gradient.
-
-    A difference counts only when both of its pixels are in the mask, so the
-    fixed exterior adds no penalty (fdtd2d/inversion/misfit.py:19-44).
-    """
-    g = np.zeros_like(m, dtype=float)
+    """0.5 * alpha * (sum of squared forward differences of m whose two pixels are
+    inside the mask) and its gradient, zero outside the mask. Computed on the GPU."""
     if alpha <= 0.0:
-        return 0.0, g
-    value = 0.0
-    for axis in (1, 0):
-        d = np.diff(m, axis=axis)
-        both = np.logical_and(np.take(mask, range(1, m.shape[axis]), axis=axis),
-                              np.take(mask, range(0, m.shape[axis] - 1), axis=axis))
-        value += 0.5 * alpha * float(np.sum(d[both] ** 2))
-        flux = np.where(both, alpha * d, 0.0)
-        if axis == 1:
-            g[:, 1:] += flux
-            g[:, :-1] -= flux
-        else:
-            g[1:, :] += flux
-            g[:-1, :] -= flux
-    g[~mask] = 0.0
-    return value, g
+        return 0.0, np.zeros(np.shape(m))
+    return regularizers(m, mask, float(alpha), 0.0, 1.0)
 
 
 def total_variation(m, mask, alpha, eps):
-    """Smoothed isotropic TV alpha * sum(sqrt(|grad m|^2 + eps^2) - eps) and its gradient
-    (fdtd2d/inversion/misfit.py:47-71)."""
-    g = np.zeros_like(m, dtype=float)
+    """alpha * sum(sqrt(|grad m|^2 + eps^2) - eps) over in-mask forward differences,
+    and its gradient, zero outside the mask. Computed on the GPU."""
     if alpha <= 0.0:
-        return 0.0, g
-    gx = np.zeros_like(m, dtype=float)
-    gy = np.zeros_like(m, dtype=float)
-    gx[:, :-1] = np.where(mask[:, 1:] & mask[:, :-1], np.diff(m, axis=1), 0.0)
-    gy[:-1, :] = np.where(mask[1:, :] & mask[:-1, :], np.diff(m, axis=0), 0.0)
-    norm = np.sqrt(gx * gx + gy * gy + eps * eps)
-    value = alpha * float(np.sum(norm - eps))
-    px = alpha * gx / norm
-    py = alpha * gy / norm
-    g -= px + py
-    g[:, 1:] += px[:, :-1]
-    g[1:, :] += py[:-1, :]
-    g[~mask] = 0.0
-    return value, g
+        return 0.0, np.zeros(np.shape(m))
+    return regularizers(m, mask, 0.0, float(alpha), float(eps))

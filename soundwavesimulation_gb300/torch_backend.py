@@ -616,14 +616,22 @@ def simulate_shots_batch(solver: TorchFDTD2D, sampler: TorchRingSampler, pulse, 
 
 
 def auto_batch_size(device, n_shots, bytes_per_shot, fallback=16, memory_fraction=0.75):
-    """Largest even split of n_shots that fits in device memory (fdtd2d/torch_backend.py:773-789)."""
+    """Shots per batch for ``n_shots`` shots of ``bytes_per_shot`` device bytes each.
+
+    The contract of fdtd2d/torch_backend.py:773-789: the budget is
+    ``memory_fraction`` of what the device can still hand out (free memory plus
+    the caching allocator's reserved but unused bytes); the shots are split into
+    the fewest batches whose size fits the budget, and the batches are made as
+    equal as possible. Off CUDA the budget is ``fallback`` shots.
+    """
+    total = int(n_shots)
     device = torch.device(device)
-    if device.type != "cuda":
-        limit = fallback
-    else:
+    if device.type == "cuda":
         free, _ = torch.cuda.mem_get_info(device)
-        cached = torch.cuda.memory_reserved(device) - torch.cuda.memory_allocated(device)
-        limit = int(memory_fraction * (free + cached) // max(int(bytes_per_shot), 1))
-    limit = max(1, min(int(n_shots), limit))
-    n_batches = -(-int(n_shots) // limit)
-    return -(-int(n_shots) // n_batches)
+        idle = torch.cuda.memory_reserved(device) - torch.cuda.memory_allocated(device)
+        fits = int((free + idle) * memory_fraction) // max(int(bytes_per_shot), 1)
+    else:
+        fits = int(fallback)
+    fits = min(total, max(fits, 1))
+    batches = math.ceil(total / fits)
+    return math.ceil(total / batches)

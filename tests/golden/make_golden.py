@@ -1,9 +1,16 @@
 """Generate the golden fixtures in this folder by running the reference itself.
 
-Run in a container that has the reference checkout (scjoshi/SoundWaveSimulation)
-at ``REFERENCE`` below:
+Run in a container that has a checkout of the reference
+(scjoshi/SoundWaveSimulation), giving its path as an argument or in the
+``SWS_REFERENCE`` environment variable:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference PATH [--cases engine,optim]
+
+``engine`` writes the engine fixtures (cases A-G below); ``optim`` writes
+``optim.npz``: the reference's Tikhonov and total-variation regularisers
+(fdtd2d/inversion/misfit.py:19-71) on a seeded model, and its projected Adam
+(invert_ring.py:817-861) for one to three iterations on a fixed quadratic
+objective.
 
 The reference is imported read-only. Its drivers import matplotlib at module top
 level (invert_ring.py:15), which is absent here, so a stub package that only
@@ -18,13 +25,14 @@ pinned against (``tests/test_oracle_golden.py``); the GPU machine never runs this.
 
 from __future__ import annotations
 
+import argparse
+import os
 import sys
 import tempfile
 from pathlib import Path
 
 import numpy as np
 
-REFERENCE = Path("/root/reference")
 OUT = Path(__file__).resolve().parent
 
 
@@ -68,9 +76,69 @@ def ellipse_medium(n, dx, n_ellipses, seed, c0=1500.0, c_lo=1430.0, c_hi=1620.0)
     return c
 
 
+def optimizer_cases() -> None:
+    """optim.npz: the reference's regularisers and projected Adam on seeded inputs."""
+    from fdtd2d.inversion import interior_mask, m_from_c
+    from fdtd2d.inversion.misfit import tikhonov, total_variation
+    from invert_ring import adam
+
+    rng = np.random.default_rng(17)
+    n, sp = 37, 1.5e-3
+    x = (np.arange(n) - 0.5 * (n - 1)) * sp
+    mask = interior_mask(x, x, 0.024, margin_m=sp)
+    c = np.full((n, n), 1500.0)
+    c[mask] = 1500.0 + 60.0 * rng.standard_normal(int(mask.sum()))
+    m = m_from_c(c)
+    alpha, tv, tv_eps = 3.0e10, 2.0e4, 1.0e-9
+    tik_value, tik_grad = tikhonov(m.copy(), mask, alpha)
+    tv_value, tv_grad = total_variation(m.copy(), mask, tv, tv_eps)
+    # projected Adam on J(m) = 0.5 * sum(w * (m - target)^2) over the mask
+    c_min, c_max, c_bg = 1400.0, 1700.0, 1500.0
+    target = m_from_c(np.where(mask, 1500.0 + 80.0 * rng.standard_normal((n, n)), c_bg))
+    weight = 1.0 + rng.random((n, n))
+
+    def project(mm):
+        out = np.clip(mm, 1.0 / c_max ** 2, 1.0 / c_min ** 2)
+        out[~mask] = 1.0 / c_bg ** 2
+        return out
+
+    def misfit_and_grad(mm):
+        r = np.where(mask, mm - target, 0.0)
+        return 0.5 * float(np.sum(weight * r * r)), weight * r
+
+    lr = 2.0e-9
+    iterates = []
+    for k in (1, 2, 3):
+        m_k, _ = adam(m.copy(), misfit_and_grad, project, mask, lr, max_iter=k, verbose=False)
+        iterates.append(m_k)
+    np.savez_compressed(
+        OUT / "optim.npz", m=m, mask=mask, alpha=alpha, tv=tv, tv_eps=tv_eps,
+        tikhonov_value=tik_value, tikhonov_grad=tik_grad, tv_value=tv_value, tv_grad=tv_grad,
+        adam_target=target, adam_weight=weight, adam_lr=lr, adam_c_min=c_min, adam_c_max=c_max,
+        adam_c_background=c_bg, adam_iterates=np.stack(iterates),
+    )
+
+
 def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("SWS_REFERENCE"),
+                    help="path of the reference checkout (default: $SWS_REFERENCE)")
+    ap.add_argument("--cases", default="engine,optim")
+    args = ap.parse_args()
+    if not args.reference:
+        ap.error("give the reference checkout with --reference or SWS_REFERENCE")
     _install_matplotlib_stub()
-    sys.path.insert(0, str(REFERENCE))
+    sys.path.insert(0, str(Path(args.reference).resolve()))
+    cases = set(args.cases.split(","))
+    if "optim" in cases:
+        optimizer_cases()
+    if "engine" in cases:
+        engine_cases(Path(args.reference).resolve())
+    for p in sorted(OUT.glob("*.npz")):
+        print(f"{p.name}: {p.stat().st_size / 1024:.1f} KB")
+
+
+def engine_cases(reference: Path) -> None:
     import torch
     from fdtd2d import ArcArray, RingArray, axis_centers, n_steps_for_crossing, stable_dt
     from fdtd2d.inversion import interior_mask, m_from_c, c_from_m
@@ -258,12 +326,11 @@ def main() -> None:
     import importlib.util
 
     def load_script(name, file):
-        spec = importlib.util.spec_from_file_location(name, REFERENCE / file)
+        spec = importlib.util.spec_from_file_location(name, reference / file)
         mod = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(mod)
         return mod
 
-    sys.path.insert(0, str(REFERENCE))
     arc_fwi = load_script("ref_invert_arc", "invert_arc.py")
     arc_cli = load_script("ref_arc_cli", "2DArcFDTD.py")
     ring_cli = load_script("ref_ring_cli", "2DRingFDTD.py")
@@ -327,8 +394,6 @@ def main() -> None:
         OUT / "multiscale.npz", m=m_g, sx=sx, sy=sx, tx=tx_g, ty=ty_g, background=1.0 / 1500.0 ** 2,
         resized=resized, stages_on=np.array(multiscale_stages(True)), stages_off=np.array(multiscale_stages(False)),
     )
-    for p in sorted(OUT.glob("*.npz")):
-        print(f"{p.name}: {p.stat().st_size / 1024:.1f} KB")
 
 
 if __name__ == "__main__":

@@ -82,18 +82,44 @@ def test_record_adjoint_is_transpose():
     assert np.dot(ring.record(f), r) == pytest.approx(np.sum(f * ring.record_adjoint(r)), rel=1e-12)
 
 
-def test_regularisers_gradients():
-    from soundwavesimulation_gb300 import interior_mask, m_from_c, tikhonov, total_variation, axis_centers
+def test_oracle_regularisers_gradients():
+    """The oracle's regularisers are consistent: central differences of the value
+    along a random in-mask direction equal the gradient's projection."""
+    from oracle import fdtd_oracle as orc
     rng = np.random.default_rng(1)
-    ax = axis_centers(41, 2e-3)
-    mask = interior_mask(ax, ax, 0.03, 0.0)
-    m = m_from_c(np.where(mask, 1500.0 + 100.0 * rng.standard_normal((41, 41)), 1500.0))
+    ax = orc.axis_centers(41, 2e-3)
+    mask = orc.interior_mask(ax, ax, 0.03, 0.0)
+    m = 1.0 / np.where(mask, 1500.0 + 100.0 * rng.standard_normal((41, 41)), 1500.0) ** 2
     d = np.where(mask, rng.standard_normal((41, 41)), 0.0) * 1e-9
-    for fn, args in ((tikhonov, (1e10,)), (total_variation, (1.0, 1e-9))):
+    for fn, args in ((orc.tikhonov, (1e10,)), (orc.total_variation, (1.0, 1e-9))):
         v, g = fn(m, mask, *args)
         fd = (fn(m + 1e-3 * d, mask, *args)[0] - fn(m - 1e-3 * d, mask, *args)[0]) / 2e-3
         assert fd == pytest.approx(np.sum(g * d), rel=1e-6)
         assert np.all(g[~mask] == 0.0) and v > 0.0
+
+
+def test_medium_helpers_match_reference_definitions(golden):
+    """m <-> c, clipping and the interior mask of the product follow the reference's
+    definitions (fdtd2d/inversion/medium.py:15-40); the ring41 fixture holds the
+    reference's own mask."""
+    from soundwavesimulation_gb300 import c_from_m, clip_m, interior_mask, m_from_c
+    from soundwavesimulation_gb300 import axis_centers, mute_transmitter, waveform_misfit
+    c = np.array([[1400.0, 1500.0], [1600.0, 2100.0]])
+    assert np.array_equal(m_from_c(c), 1.0 / (c * c))
+    assert np.allclose(c_from_m(m_from_c(c)), c, rtol=1e-15)
+    clipped = c_from_m(clip_m(m_from_c(c), 1450.0, 2000.0))
+    assert np.allclose(clipped, [[1450.0, 1500.0], [1600.0, 2000.0]], rtol=1e-15)
+    g = golden("ring41")
+    x = axis_centers(41, 2.0e-3)
+    assert np.array_equal(interior_mask(x, x, 0.030, margin_m=2 * 2.0e-3), g["mask"])
+    with pytest.raises(ValueError):
+        interior_mask(x, x, 0.01, 0.02)
+    rng = np.random.default_rng(2)
+    pred, obs = rng.standard_normal((5, 7)), rng.standard_normal((5, 7))
+    r = pred - obs
+    r[3] = 0.0
+    assert waveform_misfit(pred, obs, 3) == pytest.approx(0.5 * np.sum(r * r), rel=1e-14)
+    assert np.array_equal(mute_transmitter(pred, 3)[3], np.zeros(7))
 
 
 @pytest.mark.parametrize("n", [8, 9, 41, 64, 100, 127, 128, 129, 200, 255, 256, 257, 384, 511, 512, 1024])
@@ -155,3 +181,40 @@ def test_engine_refuses_cpu_device():
     from soundwavesimulation_gb300 import torch_backend as tb
     with pytest.raises((ValueError, RuntimeError)):
         tb.TorchScalarWave2D(np.full((16, 16), 1500.0), 1e-3, device="cpu")
+
+
+def _fake_problem(wave=0, row=20, col=20, rx_row=10, n=64):
+    """A problem description whose device pointers are placeholders: only the
+    host-side argument checks run on it (they return before any device work)."""
+    from soundwavesimulation_gb300 import _lib
+    keep = {
+        "row0": np.array([rx_row, 30], dtype=np.int32), "col0": np.array([10, 30], dtype=np.int32),
+        "w": np.full(8, 0.25, dtype=np.float32), "srow": np.array([row, 5], dtype=np.int32),
+        "scol": np.array([col, 5], dtype=np.int32), "sw": np.ones(2, dtype=np.float32),
+        "swave": np.array([wave, -1], dtype=np.int32),
+    }
+    grid = _lib.Grid(n, n, n, 1e-3, 1e-3, 1e-7, 0x1000, 0x2000)
+    rx = _lib.Receivers(2, keep["row0"].ctypes.data, keep["col0"].ctypes.data, keep["w"].ctypes.data)
+    src = _lib.Sources(2, keep["srow"].ctypes.data, keep["scol"].ctypes.data, keep["sw"].ctypes.data,
+                       keep["swave"].ctypes.data, 0x3000, 1, 100)
+    return _lib.Problem(grid, 1, 10, rx, src), keep
+
+
+@pytest.mark.parametrize("bad", [dict(wave=1), dict(wave=7), dict(row=64), dict(col=-1), dict(rx_row=63)])
+def test_plain_entry_points_validate_sources_and_receivers(bad):
+    """fdtd_forward_plain, fdtd_gradient_plain and fdtd_forward_plain_static return
+    FDTD_ERR_INVALID for an out-of-range waveform index, source node or receiver
+    before touching the device (the placeholder pointers are never dereferenced)."""
+    import ctypes
+    from soundwavesimulation_gb300 import _lib
+    lib = _lib.load()
+    prob, keep = _fake_problem(**bad)
+    assert lib.fdtd_forward_plain(ctypes.byref(prob), 0x4000, 0x5000, 1 << 40, None) == 1
+    assert lib.fdtd_forward_plain_static(ctypes.byref(prob), 0x4000, None) == 1
+    msg = lib.fdtd_last_error().decode()
+    assert "outside the grid" in msg or "waveform index" in msg, msg
+    assert lib.fdtd_gradient_plain(ctypes.byref(prob), 0x4000, None, 0x6000, 0x7000, 0x5000, 1 << 40,
+                                   None) == 1
+    prob_ok, keep_ok = _fake_problem()
+    # a valid problem passes the checks and fails only on the too-small workspace
+    assert lib.fdtd_forward_plain(ctypes.byref(prob_ok), 0x4000, 0x5000, 16, None) == 3

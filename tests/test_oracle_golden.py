@@ -194,3 +194,32 @@ def test_multiscale_stage_ladder(golden):
     d = golden("multiscale")
     np.testing.assert_array_equal(np.array(multiscale_stages(True)), d["stages_on"])
     np.testing.assert_array_equal(np.array(multiscale_stages(False)), d["stages_off"])
+
+
+def test_regularisers_and_adam_match_reference(golden):
+    """optim.npz holds the reference's tikhonov / total_variation
+    (fdtd2d/inversion/misfit.py:19-71) on a seeded model and the iterates of its
+    projected adam (invert_ring.py:817-861) on a fixed quadratic objective."""
+    g = golden("optim")
+    mask = g["mask"]
+    v, gr = orc.tikhonov(g["m"], mask, float(g["alpha"]))
+    assert v == pytest.approx(float(g["tikhonov_value"]), rel=1e-14)
+    np.testing.assert_allclose(gr, g["tikhonov_grad"], rtol=0, atol=1e-14 * np.abs(g["tikhonov_grad"]).max())
+    v, gr = orc.total_variation(g["m"], mask, float(g["tv"]), float(g["tv_eps"]))
+    assert v == pytest.approx(float(g["tv_value"]), rel=1e-14)
+    np.testing.assert_allclose(gr, g["tv_grad"], rtol=0, atol=1e-14 * np.abs(g["tv_grad"]).max())
+    lo, hi, bg = 1.0 / float(g["adam_c_max"]) ** 2, 1.0 / float(g["adam_c_min"]) ** 2, 1.0 / float(
+        g["adam_c_background"]) ** 2
+
+    def project(mm):
+        out = np.clip(mm, lo, hi)
+        out[~mask] = bg
+        return out
+
+    def objective(mm):
+        r = np.where(mask, mm - g["adam_target"], 0.0)
+        return 0.5 * float(np.sum(g["adam_weight"] * r * r)), g["adam_weight"] * r
+
+    its = orc.projected_adam(g["m"], objective, project, mask, float(g["adam_lr"]), 3)
+    for k, (mine, ref) in enumerate(zip(its, g["adam_iterates"])):
+        np.testing.assert_allclose(mine, ref, rtol=1e-14, atol=0, err_msg=f"iteration {k + 1}")

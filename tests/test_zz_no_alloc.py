@@ -75,3 +75,20 @@ def test_static_scratch_rejects_oversized_problem(setup):
                                               torch.cuda.current_stream().cuda_stream)
     assert rc == 3  # FDTD_ERR_WORKSPACE, rejected before any device work
     assert b"fixed" in lib.load().fdtd_last_error()
+
+
+def test_static_scratch_rejects_bad_waveform_index(setup):
+    """A source entry naming a waveform the table does not hold is refused with
+    FDTD_ERR_INVALID before any device work: the traces stay untouched."""
+    lib, tables, _ = setup
+    from soundwavesimulation_gb300.engine import ProblemTables
+    bad = ProblemTables.__new__(ProblemTables)
+    bad.__dict__.update(tables.__dict__)
+    bad._s_wave = tables._s_wave.copy()
+    bad._s_wave[1, 0] = 5  # the table holds one waveform
+    traces = torch.full((3, 20, 4), float("nan"), device="cuda")
+    rc = _call(lib, bad, traces)
+    torch.cuda.synchronize()
+    assert rc == 1
+    assert b"waveform index" in lib.load().fdtd_last_error()
+    assert torch.isnan(traces).all()
