@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 2
+#define FDTD_ABI_VERSION 3
 
 enum {
   FDTD_OK = 0,
@@ -271,6 +271,29 @@ size_t fdtd_gradient_plain_workspace(const fdtd_problem* problem);
    keeps the last call's contents (each shot clears the fields it uses); calls
    that overlap on the GPU race on it. */
 int32_t fdtd_forward_plain_static(const fdtd_problem* problem, float* traces, void* stream);
+
+/* ------------------------------------------------------- launch-shape search */
+
+/* Device bytes fdtd_autotune needs for this problem: the largest probe plan's
+   workspace plus its traces and a gradient buffer. */
+size_t fdtd_autotune_workspace_bytes(const fdtd_problem* problem, int32_t for_gradient, int32_t launches);
+
+/* Times every candidate launch shape (rows per lane 8 x 16 / 12 / 10 warps and
+   4 x 32 / 16 warps, steps per launch 6 .. 23) that the planner accepts for this
+   grid on `launches` temporal blocks of the problem (a forward; with
+   for_gradient a forward with checkpoints plus the adjoint), each after one
+   untimed pass, averaged over `repeats` passes with CUDA events on `stream`, and
+   writes the fastest into *best (its rate in Gcell-updates/s into *best_rate,
+   nullable). Optional report: on input *n_tried is the capacity of tried /
+   rates (nullable), on output the number written. The workspace (device, 256-
+   byte aligned, fdtd_autotune_workspace_bytes) is reused by every probe; the
+   call allocates no device memory and synchronises `stream`.
+   The reference has no tuner: its batch size comes from auto_batch_size
+   (fdtd2d/torch_backend.py:773-789) and its step from torch.compile
+   (fdtd2d/torch_backend.py:257-262). */
+int32_t fdtd_autotune(const fdtd_problem* problem, int32_t for_gradient, int32_t launches, int32_t repeats,
+                      void* workspace, size_t bytes, fdtd_tuning* best, double* best_rate,
+                      fdtd_tuning* tried, double* rates, int32_t* n_tried, void* stream);
 
 /* ------------------------------------------------------- tiling (host) */
 

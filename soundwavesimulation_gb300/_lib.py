@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "libfdtd_gb300.so"
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 
@@ -97,6 +97,10 @@ _SIGNATURES = {
     "fdtd_forward_plain_static": (c_int32, [POINTER(Problem), c_void_p, c_void_p]),
     "fdtd_tile_axis": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32, c_int32,
                                  c_void_p, POINTER(c_int32)]),
+    "fdtd_autotune_workspace_bytes": (c_size_t, [POINTER(Problem), c_int32, c_int32]),
+    "fdtd_autotune": (c_int32, [POINTER(Problem), c_int32, c_int32, c_int32, c_void_p, c_size_t,
+                                POINTER(Tuning), POINTER(c_double), c_void_p, c_void_p, POINTER(c_int32),
+                                c_void_p]),
 }
 
 EXPORTED = tuple(_SIGNATURES)

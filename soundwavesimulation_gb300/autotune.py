@@ -10,12 +10,14 @@ the autotuner measures instead of modelling.
 
 from __future__ import annotations
 
+import ctypes
 import sys
 import time
 
 import torch
 
-from .engine import FusedPlan
+from . import _lib
+from .engine import ProblemTables, ptr, stream_handle
 
 _CACHE: dict = {}
 
@@ -33,60 +35,45 @@ def autotune(medium, receivers, sources, waveforms, n_steps, launches=3, repeats
              depths=DEPTHS, verbose=False, for_gradient=False):
     """Fastest tuning dict for this acquisition; probes ``launches`` temporal blocks per shape.
 
-    With ``for_gradient`` each probe is a whole gradient pass (forward with
+    The search runs in the engine library (``fdtd_autotune``) over the candidate
+    shapes above, with one workspace from the caching allocator. With
+    ``for_gradient`` each probe is a whole gradient pass (forward with
     checkpoints, recompute and adjoint launches), since the adjoint kernel
     prefers other shapes than the forward (its coefficient tile is read
     through L1, so its shared-memory footprint matters).
     """
+    if tuple(shapes) != SHAPES or tuple(depths) != DEPTHS:
+        raise ValueError("the library searches the standard shape and depth sets")
     dev = medium.device
     n_shots = len(sources[0])
-    key = (medium.ny, medium.nx, n_shots, len(receivers[0]), str(dev), shapes, depths, bool(for_gradient))
+    key = (medium.ny, medium.nx, n_shots, len(receivers[0]), str(dev), bool(for_gradient), int(n_steps))
     if key in _CACHE:
         return dict(_CACHE[key])
-    best, best_rate, report = None, 0.0, []
+    lib = _lib.load()
+    tables = ProblemTables(medium, receivers, sources, waveforms, n_steps)
+    prob = tables.problem()
     t_start = time.perf_counter()
-    for cand in candidates(shapes, depths):
-        steps = min(int(n_steps), launches * cand["steps_per_launch"])
-        try:
-            plan = FusedPlan(medium, receivers, sources, waveforms, steps, tuning=cand,
-                             for_gradient=for_gradient)
-        except ValueError:
-            continue  # shape not supported for this grid (tiling or shared memory)
-        traces = plan.forward()
-        grad = None
-        if for_gradient:
-            grad = torch.zeros((medium.ny, medium.pitch), dtype=torch.float64, device=dev)
-
-        def one_pass():
-            if for_gradient:
-                plan.forward(traces, save_checkpoints=True)
-                plan.adjoint(traces, grad)  # any residual: the cost does not depend on its values
-            else:
-                plan.forward(traces)
-
-        one_pass()
-        torch.cuda.synchronize(dev)
-        stream = torch.cuda.current_stream(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(repeats):
-            one_pass()
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / repeats
-        rate = float(medium.ny) * medium.nx * n_shots * steps / (ms * 1e-3) / 1e9
-        report.append((rate, cand))
-        if rate > best_rate:
-            best, best_rate = dict(cand), rate
-        del plan, traces, grad
-    if best is None:
+    nbytes = int(lib.fdtd_autotune_workspace_bytes(ctypes.byref(prob), int(bool(for_gradient)), launches))
+    if nbytes == 0:
         raise RuntimeError("no candidate launch shape fits this problem")
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    cap = len(SHAPES) * len(DEPTHS)
+    tried = (_lib.Tuning * cap)()
+    rates = (ctypes.c_double * cap)()
+    n_tried = ctypes.c_int32(cap)
+    best = _lib.Tuning()
+    best_rate = ctypes.c_double()
+    _lib.check(lib.fdtd_autotune(ctypes.byref(prob), int(bool(for_gradient)), launches, repeats, ptr(ws), nbytes,
+                                 ctypes.byref(best), ctypes.byref(best_rate), tried, rates, ctypes.byref(n_tried),
+                                 stream_handle(dev)), "autotune")
+    chosen = {k: best.as_dict()[k] for k in ("rows_per_lane", "warps", "steps_per_launch")}
     if verbose:
-        for rate, cand in sorted(report, key=lambda r: -r[0])[:8]:
-            print(f"  {rate:8.1f} Gcell/s  {cand}", file=sys.stderr)
-        print(f"  autotune: {len(report)} shapes in {time.perf_counter() - t_start:.1f} s", file=sys.stderr)
-    _CACHE[key] = dict(best)
-    return best
+        report = sorted(((rates[i], tried[i].as_dict()) for i in range(n_tried.value)), key=lambda r: -r[0])
+        for rate, t in report[:8]:
+            print(f"  {rate:8.1f} Gcell/s  { {k: t[k] for k in chosen} }", file=sys.stderr)
+        print(f"  autotune: {n_tried.value} shapes in {time.perf_counter() - t_start:.1f} s", file=sys.stderr)
+    _CACHE[key] = dict(chosen)
+    return chosen
 
 
 def clear_cache():

@@ -7,9 +7,11 @@ and step counts (shot counts cut where a property does not depend on them):
   steps): the three grids in shared launches equal each grid run alone (traces
   bitwise, gradients to float64 summation order);
 * configuration 5 (1024^2, 6000 steps, 8 of the 256 shots): the gradient with
-  float16 checkpoints within 1e-3 of float32 checkpoints (bfloat16: 1.5e-2), and
-  the float32 checkpointed gradient equal to the plain full-history form of one
-  shot (1e-6).
+  float16 checkpoints within 1e-3 of float32 checkpoints, and the float32
+  checkpointed gradient equal to the plain full-history form of one shot (1e-6).
+
+Every configuration's error against float64 at full size is in
+tests/test_zy_fullsize_fp64.py.
 """
 
 import numpy as np
@@ -86,7 +88,7 @@ def test_config5_checkpoint_precision_and_plain_form(eng):
     start = engine.DeviceMedium(np.where(acq.c > 1500.0, 0.5 * (acq.c + 1500.0), acq.c), acq.dx, acq.dx,
                                 acq.dt, "cuda")
     grads = {}
-    for store in (0, 1, 2):  # float32, float16, bfloat16 checkpoints
+    for store in (0, 1):  # float32, float16 checkpoints
         plan = _plan(engine, acq, start, n_shots=S, tuning={"ckpt_store": store}, for_gradient=True)
         tr = plan.forward(save_checkpoints=True)
         res, _ = engine.residual_misfit(tr, observed, torch.as_tensor(sub.tx, dtype=torch.int32, device="cuda"))
@@ -95,10 +97,8 @@ def test_config5_checkpoint_precision_and_plain_form(eng):
         grads[store] = g.cpu().numpy()
         del plan, tr, res
         torch.cuda.empty_cache()
-    # float16 (11-bit significand) meets the 1e-3 gradient budget at this size;
-    # bfloat16 (8-bit significand) lands near 7e-3 over 6000 steps
+    # float16 (11-bit significand) meets the 1e-3 gradient budget at this size
     assert rel(grads[1], grads[0]) < 1e-3, rel(grads[1], grads[0])
-    assert rel(grads[2], grads[0]) < 1.5e-2, rel(grads[2], grads[0])
     # one shot: checkpointed float32 gradient vs the plain full-history per-step form
     one = acq.subset(n_shots=1)
     waves = torch.as_tensor(one.wavelet[None], dtype=torch.float32, device="cuda")

@@ -317,3 +317,23 @@ def test_plan_group_matches_separate_plans(tb, shape):
         g_ref = torch.zeros_like(g)
         plan.adjoint(residual_misfit(ref, torch.zeros_like(ref), None)[0], g_ref)
         assert rel(g.cpu().numpy(), g_ref.cpu().numpy()) < 1e-12
+
+
+@pytest.mark.parametrize("for_gradient", [False, True])
+def test_library_autotuner_picks_a_working_shape(tb, for_gradient):
+    """fdtd_autotune (the C-ABI launch-shape search) reports every shape it timed,
+    returns the fastest of them, and the chosen shape reproduces the default
+    shape's traces bit for bit."""
+    from soundwavesimulation_gb300.autotune import autotune, clear_cache
+    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan
+    p = _random_problem(200, 180, 3, 20, 60, seed=11, per_shot=1)
+    medium = DeviceMedium(p["c"], p["dx"], p["dy"], p["dt"], "cuda")
+    waves = torch.as_tensor(p["waves"], dtype=torch.float32, device="cuda")
+    rx = (p["row0"], p["col0"], p["w"])
+    src = (p["srow"], p["scol"], p["sw"], p["wave"])
+    clear_cache()
+    best = autotune(medium, rx, src, waves, 60, launches=2, repeats=1, for_gradient=for_gradient)
+    assert best["rows_per_lane"] in (4, 8) and 6 <= best["steps_per_launch"] <= 23
+    ref = FusedPlan(medium, rx, src, waves, 60).forward()
+    got = FusedPlan(medium, rx, src, waves, 60, tuning=best).forward()
+    assert torch.equal(ref, got)

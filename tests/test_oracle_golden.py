@@ -223,3 +223,51 @@ def test_regularisers_and_adam_match_reference(golden):
     its = orc.projected_adam(g["m"], objective, project, mask, float(g["adam_lr"]), 3)
     for k, (mine, ref) in enumerate(zip(its, g["adam_iterates"])):
         np.testing.assert_allclose(mine, ref, rtol=1e-14, atol=0, err_msg=f"iteration {k + 1}")
+
+
+def _c_receivers(d, prefix=""):
+    w = np.stack([d[prefix + k] for k in ("w00", "w10", "w01", "w11")], axis=1)
+    return d[prefix + "row0"], d[prefix + "col0"], w
+
+
+def test_c_oracle_matches_reference_ring41(golden):
+    """The float64 C oracle (oracle/fdtd_oracle.c) reproduces the reference's
+    traces, misfit and g_{c^2} of its own 41^2 problem, at any checkpoint spacing."""
+    from oracle import c_oracle
+    d = golden("ring41")
+    nt = int(d["n_steps"])
+    dx, dy, dt = float(d["dx"]), float(d["dy"]), float(d["dt"])
+    rows, cols = d["rows"][:, None], d["cols"][:, None]
+    src = (rows, cols, np.ones(rows.shape))
+    values = np.pad(d["pulse"], (0, nt - d["pulse"].size))
+    traces = c_oracle.forward_shots(d["c_true"], dx, dy, dt, src, _c_receivers(d), values, nt)
+    assert rel(traces, d["batched_traces"]) < 1e-12
+    for ckpt in (None, 5, nt):
+        J, g = c_oracle.gradient_shots(d["c_m0"], dx, dy, dt, src, _c_receivers(d), values, nt, d["observed"],
+                                       np.arange(6), ckpt_every=ckpt)
+        assert J == pytest.approx(float(d["residual_misfit"]), rel=1e-12)
+        assert rel(g, d["g_c2"]) < 1e-10
+
+
+def test_c_oracle_matches_numpy_oracle_bilinear_nonsquare():
+    """Non-square grid, dx != dy, 4-node bilinear sources: C and NumPy oracles agree."""
+    from oracle import c_oracle
+    rng = np.random.default_rng(9)
+    ny, nx, dx, dy, nt = 53, 47, 0.6e-3, 0.5e-3, 180
+    c = 1500.0 + 120.0 * rng.random((ny, nx))
+    dt = orc.stable_dt(c.max(), dx, dy, 0.35)
+    geo = orc.ring_geometry(10, 0.011, orc.axis_centers(nx, dx), orc.axis_centers(ny, dy))
+    taps = [orc.bilinear_source_taps(geo, t) for t in (0, 3, 7)]
+    rows, cols, w = (np.stack([t[i] for t in taps]) for i in range(3))
+    wav = np.sin(np.arange(nt) * 0.3) * np.exp(-((np.arange(nt) - 30) / 12.0) ** 2)
+    fields = orc.point_sources((ny, nx), rows, cols, w)
+    ref, *_ = orc.simulate_shots_batch(c, dx, dy, dt, geo, fields, wav, nt)
+    rx = (geo["row0"], geo["col0"], np.stack([geo[k] for k in ("w00", "w10", "w01", "w11")], axis=1))
+    out = c_oracle.forward_shots(c, dx, dy, dt, (rows, cols, w), rx, wav, nt)
+    assert rel(out, ref) < 1e-13
+    obs = ref * 0.9 + 0.01 * rng.standard_normal(ref.shape) * np.abs(ref).max()
+    J_ref, g_ref = orc.misfit_and_gradient_c2(c * 0.98, dx, dy, dt, geo, fields, wav, nt, obs, np.array([0, 3, -1]))
+    J, g = c_oracle.gradient_shots(c * 0.98, dx, dy, dt, (rows, cols, w), rx, wav, nt, obs, np.array([0, 3, -1]),
+                                   ckpt_every=13)
+    assert J == pytest.approx(J_ref, rel=1e-13)
+    assert rel(g, g_ref) < 1e-12
