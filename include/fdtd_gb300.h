@@ -99,7 +99,8 @@ typedef struct fdtd_tuning {
   int32_t steps_per_launch; /* leapfrog steps per HBM round trip (temporal block) */
   int32_t ckpt_every;       /* checkpoint spacing in steps, rounded up to a multiple of
                                steps_per_launch; 0 = about sqrt(2 nt) */
-  int32_t ckpt_store;       /* FDTD_STORE_F32 / _F16 / _BF16 */
+  int32_t ckpt_store;       /* FDTD_STORE_F32 / _F16 / _BF16; 16-bit checkpoints hold u and the
+                               step u - u_old, each with a power-of-two scale per shot */
   int32_t ctas_per_sm;      /* persistent grid = SMs * ctas_per_sm; 0 = 1 */
   int32_t eager;            /* 0 (default): fdtd_forward / fdtd_adjoint capture their launch
                                sequence once per set of output pointers and replay it as a

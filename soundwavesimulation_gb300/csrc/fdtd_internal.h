@@ -73,10 +73,16 @@ cudaError_t residual_launch(int n_shots, int n_rx, int n_steps, const float* tra
                             cudaStream_t st);
 cudaError_t chain_rule_launch(long long n, const double* g, const double* m,
                               const uint8_t* mask, double* out, cudaStream_t st);
-// 16-bit checkpoint storage with one power-of-two scale per (field, shot).
-cudaError_t quantize_launch(const float* src, void* dst, float* scales, int n_shots,
+// 16-bit checkpoint storage with one power-of-two scale per (field, shot). A slot
+// holds src, or src - minus when `minus` is set; dequantisation writes the value,
+// or base - value when `base` is set. The engine stores a checkpoint (u_old, u)
+// as u and u - u_old: the leapfrog step then keeps its own 11-bit (float16) or
+// 8-bit (bfloat16) relative precision instead of inheriting the rounding error
+// of two nearly equal fields, which cut the gradient error of 16-bit checkpoints
+// about ninefold in a float64 emulation.
+cudaError_t quantize_launch(const float* src, const float* minus, void* dst, float* scales, int n_shots,
                             long long per_shot, int store, cudaStream_t st);
-cudaError_t dequantize_launch(const void* src, const float* scales, float* dst, int n_shots,
+cudaError_t dequantize_launch(const void* src, const float* scales, const float* base, float* dst, int n_shots,
                               long long per_shot, int store, cudaStream_t st);
 
 }  // namespace fdtd

@@ -248,12 +248,18 @@ __global__ void chain_kernel(long long n, const double* g, const double* m, cons
   }
 }
 
-__global__ void amax_kernel(const float* src, long long per_shot, unsigned* amax) {
+// The value a checkpoint slot stores: the field itself, or with `minus` set the
+// difference field - minus (the leapfrog step u - u_old).
+__device__ __forceinline__ float ckpt_value(const float* src, const float* minus, long long i) {
+  return minus ? __fsub_rn(src[i], minus[i]) : src[i];
+}
+
+__global__ void amax_kernel(const float* src, const float* minus, long long per_shot, unsigned* amax) {
   const int s = blockIdx.y;
   float a = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_shot;
        i += (long long)gridDim.x * blockDim.x) {
-    a = fmaxf(a, fabsf(src[s * per_shot + i]));
+    a = fmaxf(a, fabsf(ckpt_value(src, minus, s * per_shot + i)));
   }
   for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_down_sync(0xffffffffu, a, o));
   if ((threadIdx.x & 31) == 0) atomicMax(amax + s, __float_as_uint(a));
@@ -268,7 +274,7 @@ __device__ __forceinline__ float pow2_scale(unsigned amax_bits) {
   return ldexpf(1.f, e - 15);
 }
 
-__global__ void quant_kernel(const float* src, void* dst, const unsigned* amax, float* scales,
+__global__ void quant_kernel(const float* src, const float* minus, void* dst, const unsigned* amax, float* scales,
                              long long per_shot, int store) {
   const int s = blockIdx.y;
   const float sc = pow2_scale(amax[s]);
@@ -276,7 +282,7 @@ __global__ void quant_kernel(const float* src, void* dst, const unsigned* amax, 
   const float inv = 1.f / sc;  // exact: sc is a power of two
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_shot;
        i += (long long)gridDim.x * blockDim.x) {
-    const float v = src[s * per_shot + i] * inv;
+    const float v = ckpt_value(src, minus, s * per_shot + i) * inv;
     if (store == 1) {
       reinterpret_cast<__half*>(dst)[s * per_shot + i] = __float2half_rn(v);
     } else {
@@ -285,15 +291,18 @@ __global__ void quant_kernel(const float* src, void* dst, const unsigned* amax, 
   }
 }
 
-__global__ void dequant_kernel(const void* src, const float* scales, float* dst,
+// dst = q * scale, or with `base` set dst = base - q * scale (u_old from u and u - u_old).
+__global__ void dequant_kernel(const void* src, const float* scales, const float* base, float* dst,
                                long long per_shot, int store) {
   const int s = blockIdx.y;
   const float sc = scales[s];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per_shot;
        i += (long long)gridDim.x * blockDim.x) {
-    const float q = (store == 1) ? __half2float(reinterpret_cast<const __half*>(src)[s * per_shot + i])
-                                 : __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(src)[s * per_shot + i]);
-    dst[s * per_shot + i] = q * sc;
+    const long long k = s * per_shot + i;
+    const float q = (store == 1) ? __half2float(reinterpret_cast<const __half*>(src)[k])
+                                 : __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(src)[k]);
+    const float v = q * sc;  // exact: sc is a power of two
+    dst[k] = base ? __fsub_rn(base[k], v) : v;
   }
 }
 
@@ -370,24 +379,24 @@ cudaError_t chain_rule_launch(long long n, const double* g, const double* m,
   return cudaGetLastError();
 }
 
-cudaError_t quantize_launch(const float* src, void* dst, float* scales, int n_shots,
+cudaError_t quantize_launch(const float* src, const float* minus, void* dst, float* scales, int n_shots,
                             long long per_shot, int store, cudaStream_t st) {
   // scales holds 2 * n_shots floats: [0, n) amax scratch, [n, 2n) the scales.
   unsigned* amax = reinterpret_cast<unsigned*>(scales);
   cudaError_t e = cudaMemsetAsync(amax, 0, sizeof(unsigned) * n_shots, st);
   if (e != cudaSuccess) return e;
   dim3 grid(64, n_shots);
-  amax_kernel<<<grid, 256, 0, st>>>(src, per_shot, amax);
+  amax_kernel<<<grid, 256, 0, st>>>(src, minus, per_shot, amax);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  quant_kernel<<<grid, 256, 0, st>>>(src, dst, amax, scales + n_shots, per_shot, store);
+  quant_kernel<<<grid, 256, 0, st>>>(src, minus, dst, amax, scales + n_shots, per_shot, store);
   return cudaGetLastError();
 }
 
-cudaError_t dequantize_launch(const void* src, const float* scales, float* dst, int n_shots,
+cudaError_t dequantize_launch(const void* src, const float* scales, const float* base, float* dst, int n_shots,
                               long long per_shot, int store, cudaStream_t st) {
   dim3 grid(64, n_shots);
-  dequant_kernel<<<grid, 256, 0, st>>>(src, scales + n_shots, dst, per_shot, store);
+  dequant_kernel<<<grid, 256, 0, st>>>(src, scales + n_shots, base, dst, per_shot, store);
   return cudaGetLastError();
 }
 

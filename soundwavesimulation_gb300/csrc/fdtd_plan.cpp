@@ -830,6 +830,7 @@ struct Op {
   TbParams q;
   void* dst = nullptr;
   const void* src = nullptr;
+  const float* aux = nullptr;  // QUANT: field subtracted from src; DEQUANT: base the value is subtracted from
   size_t bytes = 0;
   float* scales = nullptr;
   const float* cscales = nullptr;
@@ -842,9 +843,11 @@ int32_t exec_helper(const Op& op, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
   if (op.kind == Op::MEMSET) e = cudaMemsetAsync(op.dst, 0, op.bytes, st);
   else if (op.kind == Op::QUANT)
-    e = quantize_launch(static_cast<const float*>(op.src), op.dst, op.scales, op.n_shots, op.per_shot, op.store, st);
+    e = quantize_launch(static_cast<const float*>(op.src), op.aux, op.dst, op.scales, op.n_shots, op.per_shot,
+                        op.store, st);
   else if (op.kind == Op::DEQUANT)
-    e = dequantize_launch(op.src, op.cscales, static_cast<float*>(op.dst), op.n_shots, op.per_shot, op.store, st);
+    e = dequantize_launch(op.src, op.cscales, op.aux, static_cast<float*>(op.dst), op.n_shots, op.per_shot,
+                          op.store, st);
   return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "pass helper");
 }
 
@@ -879,10 +882,12 @@ struct Sink {
     op.bytes = bytes;
     return emit(op);
   }
-  int32_t quant(const float* src, void* dst, float* scales, int n_shots, long long per_shot, int store) {
+  int32_t quant(const float* src, const float* minus, void* dst, float* scales, int n_shots, long long per_shot,
+                int store) {
     Op op;
     op.kind = Op::QUANT;
     op.src = src;
+    op.aux = minus;
     op.dst = dst;
     op.scales = scales;
     op.n_shots = n_shots;
@@ -890,10 +895,12 @@ struct Sink {
     op.store = store;
     return emit(op);
   }
-  int32_t dequant(const void* src, const float* scales, float* dst, int n_shots, long long per_shot, int store) {
+  int32_t dequant(const void* src, const float* scales, const float* base, float* dst, int n_shots,
+                  long long per_shot, int store) {
     Op op;
     op.kind = Op::DEQUANT;
     op.src = src;
+    op.aux = base;
     op.cscales = scales;
     op.dst = dst;
     op.n_shots = n_shots;
@@ -945,10 +952,11 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
     if (ckpt && p->tun.ckpt_store != FDTD_STORE_F32) {
       const size_t eb = p->field_elems * p->ckpt_elem_bytes;
       const long long per_shot = (long long)p->prob.grid.ny * p->prob.grid.pitch;
+      // slot 0: the step u - u_old, slot 1: u
       for (int f = 0; f < 2; ++f) {
         char* dst = p->ws + p->o_ckpt + ((size_t)(j - 1) * 2 + f) * eb;
         float* sc = fptr(p, p->o_scales) + ((size_t)(j - 1) * 2 + f) * 2 * p->prob.n_shots;
-        rc = k.quant(f == 0 ? out_prev : out_cur, dst, sc, p->prob.n_shots, per_shot, p->tun.ckpt_store);
+        rc = k.quant(out_cur, f == 0 ? out_prev : nullptr, dst, sc, p->prob.n_shots, per_shot, p->tun.ckpt_store);
         if (rc) return rc;
       }
     }
@@ -992,11 +1000,12 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Si
       in_set = -1;
     } else {
       const size_t eb = p->field_elems * p->ckpt_elem_bytes;
-      for (int f = 0; f < 2; ++f) {
+      // u first (slot 1), then u_old = u - (u - u_old) (slot 0)
+      for (int f = 1; f >= 0; --f) {
         const char* src = p->ws + p->o_ckpt + ((size_t)(j - 1) * 2 + f) * eb;
         const float* sc = fptr(p, p->o_scales) + ((size_t)(j - 1) * 2 + f) * 2 * p->prob.n_shots;
-        const int32_t rc = k.dequant(src, sc, fptr(p, p->o_state[0][f]), p->prob.n_shots, per_shot,
-                                     p->tun.ckpt_store);
+        const int32_t rc = k.dequant(src, sc, f == 0 ? fptr(p, p->o_state[0][1]) : nullptr,
+                                     fptr(p, p->o_state[0][f]), p->prob.n_shots, per_shot, p->tun.ckpt_store);
         if (rc) return rc;
       }
       in_prev = fptr(p, p->o_state[0][0]);

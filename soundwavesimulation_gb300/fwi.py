@@ -17,7 +17,8 @@
 The imaging uses every time step, so the gradient equals the reference's with
 ``store_every = 1``. ``store_every`` is accepted for signature compatibility
 and only enters the memory estimate; ``wave_dtype`` float16 / bfloat16 selects
-16-bit checkpoint storage with one power-of-two scale per field and shot.
+16-bit checkpoint storage: u and the leapfrog step u - u_old, each with one
+power-of-two scale per shot.
 """
 
 from __future__ import annotations
