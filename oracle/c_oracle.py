@@ -46,10 +46,10 @@ def load():
         ip, dp = POINTER(c_int), POINTER(c_double)
         lib.orc_forward_shot.restype = c_int
         lib.orc_forward_shot.argtypes = [c_int, c_int, c_double, c_double, c_double, dp, c_int, ip, ip, dp, dp,
-                                         c_int, c_int, ip, ip, dp, c_int, dp]
+                                         c_int, c_int, ip, ip, dp, c_int, dp, c_int, c_double]
         lib.orc_gradient_shot.restype = c_int
         lib.orc_gradient_shot.argtypes = [c_int, c_int, c_double, c_double, c_double, dp, c_int, ip, ip, dp, dp,
-                                          c_int, c_int, ip, ip, dp, c_int, dp, c_int, c_int, dp, dp]
+                                          c_int, c_int, ip, ip, dp, c_int, dp, c_int, c_int, dp, dp, c_int, c_double]
         _lib = lib
     return _lib
 
@@ -63,17 +63,21 @@ def _dp(a):
 
 
 class _Shots:
-    """Shot tables in the C oracle's layout."""
+    """Shot tables in the C oracle's layout; with a PML of ``pml`` cells the medium
+    is padded with its edge values and every index shifted into the padded grid."""
 
-    def __init__(self, c, sources, receivers, wave):
-        self.c = np.ascontiguousarray(c, dtype=np.float64)
+    def __init__(self, c, sources, receivers, wave, pml=0):
+        c = np.asarray(c, dtype=np.float64)
+        self.pml = int(pml)
+        self.shape = c.shape
+        self.c = np.ascontiguousarray(np.pad(c, self.pml, mode="edge") if self.pml else c)
         rows, cols, w = (np.asarray(a) for a in sources)
-        self.rows = np.ascontiguousarray(rows.reshape(rows.shape[0], -1), dtype=np.int32)
-        self.cols = np.ascontiguousarray(cols.reshape(self.rows.shape), dtype=np.int32)
+        self.rows = np.ascontiguousarray(rows.reshape(rows.shape[0], -1) + self.pml, dtype=np.int32)
+        self.cols = np.ascontiguousarray(cols.reshape(self.rows.shape) + self.pml, dtype=np.int32)
         self.w = np.ascontiguousarray(np.asarray(w, dtype=np.float64).reshape(self.rows.shape))
         r0, c0, rw = receivers
-        self.r0 = np.ascontiguousarray(r0, dtype=np.int32)
-        self.c0 = np.ascontiguousarray(c0, dtype=np.int32)
+        self.r0 = np.ascontiguousarray(np.asarray(r0) + self.pml, dtype=np.int32)
+        self.c0 = np.ascontiguousarray(np.asarray(c0) + self.pml, dtype=np.int32)
         self.rw = np.ascontiguousarray(np.asarray(rw, dtype=np.float64).reshape(-1, 4))
         self.wave = np.ascontiguousarray(wave, dtype=np.float64)
         self.S, self.K = self.rows.shape
@@ -90,19 +94,21 @@ def _run(fn, n, threads):
         return list(pool.map(fn, range(n)))
 
 
-def forward_shots(c, dx, dy, dt, sources, receivers, wave, n_steps, threads=None):
+def forward_shots(c, dx, dy, dt, sources, receivers, wave, n_steps, threads=None, pml=0, pml_reflection=1e-5):
     """float64 traces (S, R, n_steps) of every shot.
 
     ``sources``: (rows, cols, weights), each (S, K) — shot s injects
     ``w * wave[step]`` at its K nodes; ``receivers``: (row0, col0, weights (R, 4)).
+    ``pml`` > 0 pads a PML of that many cells outside the grid (no Mur edges).
     """
     lib = load()
-    sh = _Shots(c, sources, receivers, wave)
+    sh = _Shots(c, sources, receivers, wave, pml)
     out = np.zeros((sh.S, len(sh.r0), int(n_steps)))
 
     def one(s):
         (ny, nx), rest = sh.args(s)
-        rc = lib.orc_forward_shot(ny, nx, dx, dy, dt, *rest, int(n_steps), _dp(out[s]))
+        rc = lib.orc_forward_shot(ny, nx, dx, dy, dt, *rest, int(n_steps), _dp(out[s]), sh.pml,
+                                  float(pml_reflection))
         if rc != 0:
             raise RuntimeError(f"oracle forward failed ({rc})")
 
@@ -111,14 +117,15 @@ def forward_shots(c, dx, dy, dt, sources, receivers, wave, n_steps, threads=None
 
 
 def gradient_shots(c, dx, dy, dt, sources, receivers, wave, n_steps, observed, mute, ckpt_every=None,
-                   threads=None):
+                   threads=None, pml=0, pml_reflection=1e-5):
     """float64 misfit and g_{c^2} (ny, nx) summed over shots (no mask, no chain rule).
 
     ``observed`` (S, R, n_steps); ``mute[s]`` is the receiver channel of shot s left
-    out of the residual (-1: none).
+    out of the residual (-1: none). With ``pml`` the gradient is returned on the
+    physical grid (the layer cropped).
     """
     lib = load()
-    sh = _Shots(c, sources, receivers, wave)
+    sh = _Shots(c, sources, receivers, wave, pml)
     obs = np.ascontiguousarray(observed, dtype=np.float64)
     mute = np.broadcast_to(np.asarray(mute, dtype=np.int64).reshape(-1), (sh.S,))
     C = int(ckpt_every or max(1, int(np.ceil(np.sqrt(2.0 * n_steps)))))
@@ -129,13 +136,16 @@ def gradient_shots(c, dx, dy, dt, sources, receivers, wave, n_steps, observed, m
         (ny, nx), rest = sh.args(s)
         j = c_double(0.0)
         rc = lib.orc_gradient_shot(ny, nx, dx, dy, dt, *rest, int(n_steps), _dp(obs[s]), int(mute[s]), C,
-                                   ctypes.byref(j), _dp(grads[s]))
+                                   ctypes.byref(j), _dp(grads[s]), sh.pml, float(pml_reflection))
         if rc != 0:
             raise RuntimeError(f"oracle gradient failed ({rc})")
         J[s] = j.value
 
     _run(one, sh.S, threads)
-    return float(J.sum()), grads.sum(axis=0)
+    g = grads.sum(axis=0)
+    if sh.pml:
+        g = g[sh.pml:sh.pml + sh.shape[0], sh.pml:sh.pml + sh.shape[1]]
+    return float(J.sum()), np.ascontiguousarray(g)
 
 
 def misfit(traces, observed, mute):

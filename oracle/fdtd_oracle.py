@@ -509,3 +509,136 @@ def projected_adam(m0, misfit_and_grad, project, mask, learning_rate, iterations
         _, g = misfit_and_grad(m)
         out.append(m.copy())
     return out
+
+
+# ---------------------------------------------------------------------------
+# PML absorbing layer (no reference counterpart: the reference has first-order
+# Mur edges only, fdtd2d/solver.py:90-124). An own float64 restatement of the
+# engine's PML, checked against a larger grid and the water line-source trace
+# of desmond/src/phase2_numerics.py:126-145.
+# ---------------------------------------------------------------------------
+
+def pml_sigma_max(cells, h, c_ref, reflection=1e-5, order=2):
+    """Peak damping of a graded layer of ``cells`` cells: (order+1) c ln(1/R) / (2 L)."""
+    return (order + 1) * c_ref * np.log(1.0 / reflection) / (2.0 * cells * h)
+
+
+def pml_profile(n, cells, h, sigma_max, order=2):
+    """Damping at cell centres ``sc[i]`` and at left faces ``sf[i]`` (face i - 1/2) of a
+    padded axis of n cells whose first and last ``cells`` cells form the layer.
+
+    Depth is measured from the layer's inner face (coordinate cells - 1/2 on the
+    low side, n - cells - 1/2 on the high side, cell i at coordinate i), in units
+    of the layer thickness: sigma = sigma_max * (depth / cells)^order.
+    """
+    def sigma(x):
+        lo = np.maximum(0.0, (cells - 0.5) - x)
+        hi = np.maximum(0.0, x - (n - cells - 0.5))
+        return sigma_max * (np.maximum(lo, hi) / cells) ** order
+    i = np.arange(n, dtype=float)
+    if cells <= 0:
+        return np.zeros(n), np.zeros(n)
+    return sigma(i), sigma(i - 0.5)
+
+
+def pml_coefficients(c, dt, dx, dy, cells, reflection=1e-5):
+    """Everything the PML update needs, in float64, for a padded medium c (ny, nx)."""
+    c = np.asarray(c, dtype=float)
+    ny, nx = c.shape
+    smax_x = pml_sigma_max(cells, dx, float(c.max()), reflection)
+    smax_y = pml_sigma_max(cells, dy, float(c.max()), reflection)
+    sxc, sxf = pml_profile(nx, cells, dx, smax_x)
+    syc, syf = pml_profile(ny, cells, dy, smax_y)
+    a = 0.5 * dt * (sxc[None, :] + syc[:, None])
+    q = 1.0 / (1.0 + a)
+    return {
+        "sxc": sxc, "sxf": sxf, "syc": syc, "syf": syf,
+        "ax": (1.0 - 0.5 * dt * sxf) / (1.0 + 0.5 * dt * sxf),   # face decay of psi_x
+        "bx": dt / (dx * dx * (1.0 + 0.5 * dt * sxf)),           # face forcing scale of psi_x
+        "ay": (1.0 - 0.5 * dt * syf) / (1.0 + 0.5 * dt * syf),
+        "by": dt / (dy * dy * (1.0 + 0.5 * dt * syf)),
+        "q": q, "A": q * (2.0 - dt * dt * sxc[None, :] * syc[:, None]), "M": (1.0 - a) * q,
+    }
+
+
+def pml_step(u_old, u, psx, psy, coef, dx, dy, p, source=None):
+    """One leapfrog step with the PML; returns (u_next, psx_next, psy_next).
+
+    The second-order PML (stretched coordinates s = 1 + sigma / (i omega) per axis,
+    multiplied through by s_x s_y):
+      u_tt + (sx + sy) u_t + sx sy u = c^2 (lap u + d/dx phi_x + d/dy phi_y),
+      phi_x_t = -sx phi_x + (sy - sx) du/dx,  phi_y_t = -sy phi_y + (sx - sy) du/dy,
+    with phi on the cell faces at half steps (trapezoidal decay), stored as
+    psi = phi / h. Here psx[..., j, i] lives on the face between cells i-1 and i
+    and psy[..., j, i] on the face between rows j-1 and j; beyond the grid u and
+    psi are zero (a rigid outer wall behind the layer). ``coef`` is (c dt)^2;
+    the update is u+ = q coef (lap u + div psi) + A u - M u- (+ sources) with
+    q = 1 / (1 + a), A = q (2 - dt^2 sx sy), M = (1 - a) q, a = dt (sx + sy) / 2,
+    which is the plain leapfrog where sigma = 0.
+    """
+    zx = np.zeros(u.shape[:-1] + (1,))
+    zy = np.zeros(u.shape[:-2] + (1, u.shape[-1]))
+    dux = np.diff(np.concatenate([zx, u], axis=-1), axis=-1)      # u_i - u_{i-1}
+    duy = np.diff(np.concatenate([zy, u], axis=-2), axis=-2)      # u_j - u_{j-1}
+    psx_n = p["ax"][None, :] * psx + (p["syc"][:, None] - p["sxf"][None, :]) * p["bx"][None, :] * dux
+    psy_n = p["ay"][:, None] * psy + (p["sxc"][None, :] - p["syf"][:, None]) * p["by"][:, None] * duy
+    div = (np.diff(np.concatenate([psx_n, zx], axis=-1), axis=-1)
+           + np.diff(np.concatenate([psy_n, zy], axis=-2), axis=-2))
+    u_next = (p["q"] * coef) * (laplacian(u, dx, dy) + div) + (p["A"] * u - p["M"] * u_old)
+    if source is not None:
+        u_next = u_next + source
+    return u_next, psx_n, psy_n
+
+
+def pad_medium(c, cells):
+    """The medium extended by ``cells`` cells on every side with its edge values."""
+    return np.pad(np.asarray(c, dtype=float), cells, mode="edge")
+
+
+def simulate_pml(c, dx, dy, dt, geo, source_fields, source_values, n_steps, cells, reflection=1e-5):
+    """Batched forward with the PML padded outside the grid: traces (S, R, n_steps)
+    at the receivers of ``geo`` (physical-grid indices), and the final physical field."""
+    cp = pad_medium(c, cells)
+    p = pml_coefficients(cp, dt, dx, dy, cells, reflection)
+    coef = (cp * dt) ** 2
+    fields = np.asarray(source_fields, dtype=float)
+    S = fields.shape[0]
+    fp = np.zeros((S,) + cp.shape)
+    fp[:, cells:cells + c.shape[0], cells:cells + c.shape[1]] = fields
+    values = np.asarray(source_values, dtype=float)
+    if values.ndim == 1:
+        values = np.broadcast_to(values, (S, values.shape[0]))
+    u_old = np.zeros((S,) + cp.shape)
+    u = np.zeros_like(u_old)
+    psx = np.zeros_like(u)
+    psy = np.zeros_like(u)
+    g = dict(geo)
+    for k in ("row0", "row1", "col0", "col1"):
+        g[k] = np.asarray(geo[k]) + cells
+    traces = np.zeros((S, len(geo["row0"]), n_steps))
+    for step in range(n_steps):
+        src = fp * values[:, step, None, None] if step < values.shape[1] else None
+        u_next, psx, psy = pml_step(u_old, u, psx, psy, coef, dx, dy, p, src)
+        u_old, u = u, u_next
+        traces[:, :, step] = gather(u, g)
+    return traces, u[:, cells:cells + c.shape[0], cells:cells + c.shape[1]]
+
+
+def analytic_line_source(r, t, h, dt_sim, pulse, c=1500.0, dt_a=None):
+    """Exact 2-D response at distance r to the solver's point source (u += pulse(t_n)
+    per step), as desmond/src/phase2_numerics.py:126-145 computes it: the source is
+    the forcing pulse(t) h^2 / dt^2 at a point, and the 2-D Green's function
+    H(t - r/c) / (2 pi c^2 sqrt(t^2 - r^2/c^2)) is integrated exactly over each fine
+    time step and convolved with the pulse. ``pulse`` is a callable of time."""
+    dt_a = dt_sim / 20.0 if dt_a is None else dt_a
+    T = r / c
+    ta = np.arange(0, t[-1] + dt_a, dt_a)
+    lo = np.maximum(ta, T)
+    hi = np.maximum(ta + dt_a, T)
+    G = np.arccosh(hi / T) - np.arccosh(lo / T)
+    s = pulse(ta + 0.5 * dt_a)
+    n = ta.size
+    m = 1 << int(np.ceil(np.log2(2 * n)))
+    u = np.fft.irfft(np.fft.rfft(s, m) * np.fft.rfft(G, m), m)[:n] / (2 * np.pi * c ** 2)
+    u *= h ** 2 / dt_sim ** 2
+    return np.interp(t, ta + dt_a, u)
