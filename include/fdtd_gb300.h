@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 3
+#define FDTD_ABI_VERSION 4
 
 enum {
   FDTD_OK = 0,
@@ -45,16 +45,25 @@ enum {
 
 enum { FDTD_STORE_F32 = 0, FDTD_STORE_F16 = 1, FDTD_STORE_BF16 = 2 };
 
-/* Grid and medium. `coef` and `mur` come from fdtd_prepare_medium. */
+/* Grid and medium. `coef` and `mur` come from fdtd_prepare_medium, or for a grid
+   with a PML layer from fdtd_prepare_medium_pml. */
 typedef struct fdtd_grid {
   int32_t ny, nx, pitch;
   double dx, dy, dt;
-  const float* coef; /* device (ny, pitch): (c * dt)^2 */
+  const float* coef; /* device (ny, pitch): (c * dt)^2; with a PML q (c * dt)^2, q = 1 / (1 + a),
+                        a = dt (sigma_x + sigma_y) / 2 */
   const float* mur;  /* device, 2 * (2 ny + 2 nx + 8) floats: k_left[ny], k_right[ny],
                         k_bottom[nx], k_top[nx], corner_kx[4], corner_ky[4] (corners
                         in the order (0,0), (0,nx-1), (ny-1,0), (ny-1,nx-1)), then in
                         the same layout the ratios coef_edge / coef_inner used by the
                         adjoint in w = coef * l form */
+  const float* pml;  /* NULL (Mur edges, the reference's boundary), or device PML tables of
+                        4 (nx + ny) floats: per column sigma_x at the cell centre, at the left
+                        face, the face decay (1 - sigma dt / 2) / (1 + sigma dt / 2) and the
+                        forcing scale dt / (dx^2 (1 + sigma dt / 2)); then per row the same
+                        for y. The grid then has no Mur edges: it ends in a rigid wall
+                        behind the layer. */
+  int32_t pml_cells; /* layer thickness in cells on every side (with pml) */
 } fdtd_grid;
 
 /* Bilinear receivers (host arrays of length n). Receiver i samples rows
@@ -121,6 +130,16 @@ int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pit
                             double dt, double dx, double dy,
                             float* coef, float* mur, void* stream);
 
+/* The same for a grid padded by a PML layer of `cells` cells on every side (no
+   reference counterpart: the reference has first-order Mur edges only). c is the
+   padded medium; the damping grows as sigma_max (depth / cells)^2 with
+   sigma_max = 3 max(c) ln(1 / reflection) / (2 cells h) per axis. Writes coef =
+   q (c dt)^2, the Mur table (unused by PML grids) and the PML tables
+   (device, 4 (nx + ny) floats) that fdtd_grid.pml points to. */
+int32_t fdtd_prepare_medium_pml(const double* c, int32_t ny, int32_t nx, int32_t pitch,
+                                double dt, double dx, double dy, int32_t cells, double reflection,
+                                float* coef, float* mur, float* pml, void* stream);
+
 /* ------------------------------------------------- one-step (plain) kernels */
 
 /* One leapfrog step for n_shots shots, Mur edges included:
@@ -141,6 +160,19 @@ int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots,
                   const float* src_w, const int32_t* src_wave,
                   const float* waveforms, int32_t waveform_len, int32_t step,
                   const float* dense, int32_t adjoint, void* stream);
+
+/* One leapfrog step of a PML grid (grid->pml set): the face fields psi_x, psi_y
+   (device (n_shots, ny, pitch), zero at the start) step from psx / psy into
+   psx_next / psy_next together with the field; no Mur edges. Sources and
+   `adjoint` (0 forward, 2 the w = coef * l adjoint) as fdtd_step. The fused
+   engine computes the same values bit for bit. No reference counterpart. */
+int32_t fdtd_step_pml(const fdtd_grid* grid, int32_t n_shots,
+                      const float* u_old, const float* u, float* u_next,
+                      const float* psx, const float* psy, float* psx_next, float* psy_next,
+                      int32_t src_per_shot, const int32_t* src_row, const int32_t* src_col,
+                      const float* src_w, const int32_t* src_wave,
+                      const float* waveforms, int32_t waveform_len, int32_t step,
+                      const float* dense, int32_t adjoint, void* stream);
 
 /* Bilinear receiver samples of a field batch:
    out[s * out_shot_stride + r * out_rx_stride] for s < n_shots, r < n_rx.

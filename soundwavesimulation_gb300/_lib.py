@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "libfdtd_gb300.so"
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 
@@ -22,7 +22,7 @@ STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 class Grid(ctypes.Structure):
     _fields_ = [("ny", c_int32), ("nx", c_int32), ("pitch", c_int32),
                 ("dx", c_double), ("dy", c_double), ("dt", c_double),
-                ("coef", c_void_p), ("mur", c_void_p)]
+                ("coef", c_void_p), ("mur", c_void_p), ("pml", c_void_p), ("pml_cells", c_int32)]
 
 
 class Receivers(ctypes.Structure):
@@ -57,6 +57,11 @@ _SIGNATURES = {
     "fdtd_step": (c_int32, [POINTER(Grid), c_int32, c_void_p, c_void_p, c_void_p, c_int32,
                             c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
                             c_void_p, c_int32, c_void_p]),
+    "fdtd_step_pml": (c_int32, [POINTER(Grid), c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_int32, c_int32, c_void_p, c_int32, c_void_p]),
+    "fdtd_prepare_medium_pml": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_double, c_double, c_double,
+                                          c_int32, c_double, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fdtd_gather": (c_int32, [POINTER(Grid), c_int32, c_void_p, c_int32, c_void_p, c_void_p,
                               c_void_p, c_int64, c_int64, c_void_p]),
     "fdtd_scatter": (c_int32, [POINTER(Grid), c_int32, c_int32, c_void_p, c_void_p, c_void_p,

@@ -70,6 +70,47 @@ __device__ __forceinline__ float inj_acc(float acc, float w, float v) {
 
 __device__ __forceinline__ float inj_add(float un, float inj) { return __fadd_rn(un, inj); }
 
+// ---------------------------------------------------------------- PML
+//
+// The second-order PML of a grid padded by a damping layer (no reference
+// counterpart; the reference has first-order Mur edges only): stretched
+// coordinates s = 1 + sigma / (i omega) per axis, multiplied through by s_x s_y,
+//   u_tt + (sx + sy) u_t + sx sy u = c^2 (lap u + d/dx phi_x + d/dy phi_y),
+//   phi_x_t = -sx phi_x + (sy - sx) du/dx,  phi_y_t = -sy phi_y + (sx - sy) du/dy,
+// with phi on the cell faces at half steps, stored as psi = phi / h: psi_x of cell
+// (y, x) lives on its left face, psi_y on its bottom face. Tables per column
+// (sigma_x at the centre and the left face, the face decay and forcing scale) and
+// per row (the same for y) come from fdtd_prepare_medium_pml; the update factors
+// of a cell follow from sigma_x, sigma_y at its centre. Where sigma = 0 every
+// factor is exactly 1 or 2 and psi stays 0, so the update is bit for bit the
+// plain leapfrog (leap above).
+
+// One face value psi+ = alpha psi + (sigma_other - sigma_face) beta du.
+__device__ __forceinline__ float pml_face(float alpha, float psi, float sig_other, float sig_face, float beta,
+                                          float du) {
+  return __fmaf_rn(alpha, psi, __fmul_rn(__fmul_rn(__fsub_rn(sig_other, sig_face), beta), du));
+}
+
+// Factors A = q (2 - dt^2 sx sy) and M = (1 - a) q, with a = dt (sx + sy) / 2 and
+// q = 1 / (1 + a), of the cell update u+ = K (lap + div) + A u - M u-, where the
+// coefficient table holds K = q (c dt)^2.
+__device__ __forceinline__ void pml_factors(float sxc, float syc, float hdt, float dt2, float& A, float& M) {
+  const float a = __fmul_rn(hdt, __fadd_rn(sxc, syc));
+  const float q = __frcp_rn(__fadd_rn(1.0f, a));
+  A = __fmul_rn(q, __fsub_rn(2.0f, __fmul_rn(dt2, __fmul_rn(sxc, syc))));
+  M = __fmul_rn(__fsub_rn(1.0f, a), q);
+}
+
+// div psi = (psi_x right - psi_x left) + (psi_y top - psi_y bottom)
+__device__ __forceinline__ float pml_div(float pxl, float pxr, float pyb, float pyt) {
+  return __fadd_rn(__fsub_rn(pxr, pxl), __fsub_rn(pyt, pyb));
+}
+
+// u+ = K (lap + div) + (A u - M u-): the plain leap when A = 2, M = 1, div = 0.
+__device__ __forceinline__ float pml_leap(float c, float p, float K, float A, float M, float lap, float div) {
+  return __fmaf_rn(K, __fadd_rn(lap, div), __fmaf_rn(A, c, -__fmul_rn(M, p)));
+}
+
 // ------------------------------------------------------------ parameters
 
 constexpr int MODE_FWD = 0;  // forward: sources in, receiver traces out
@@ -80,8 +121,13 @@ constexpr int RX = 128;       // region width: 32 lanes x 4 columns
 constexpr int TAP_C = 8;      // receivers sharing one tap node
 constexpr int SRC_C = 4;      // source entries sharing one node
 
-// Tile flags.
-constexpr int TF_LEFT = 1, TF_RIGHT = 2, TF_BOTTOM = 4, TF_TOP = 8, TF_OUTSIDE = 16;
+// Tile flags. TF_PML: the region holds cells of a PML layer.
+constexpr int TF_LEFT = 1, TF_RIGHT = 2, TF_BOTTOM = 4, TF_TOP = 8, TF_OUTSIDE = 16, TF_PML = 32;
+constexpr int TF_MUR = TF_LEFT | TF_RIGHT | TF_BOTTOM | TF_TOP;
+
+// PML tables (device, 4 (nx + ny) floats): per column sigma_x at the centre, at
+// the left face, the psi_x decay and forcing scale; then the same per row for y.
+constexpr int PML_TABLES = 4;
 
 struct TbTile {
   int rx0, ry0;          // region origin (rx0 multiple of 4)
@@ -159,6 +205,16 @@ struct TbParams {
   const float* residual;
   double* grad;
   double scale;
+  // PML (pml != nullptr): tables, update constants dt / 2 and dt^2, the face
+  // fields psi_x / psi_y in and out (nshots, ny, pitch), and the per-CTA capacity
+  // of thread slots holding a thread's face fields in shared memory
+  const float* pml;
+  float hdt, dt2;
+  const float* in_psx;
+  const float* in_psy;
+  float* out_psx;
+  float* out_psy;
+  int slot_cap;
 };
 
 // Several plans of one launch shape advanced by one launch (uneven batches).
@@ -171,13 +227,14 @@ struct TbGroup {
 // Dynamic shared-memory carve-up of the temporally blocked kernel; the host
 // sizes the launch with the same function.
 struct TbSmem {
-  size_t coef, lap, g, xch, mur, tap, res, src, mask, base, smask, sbase, total;
+  size_t coef, lap, g, xch, mur, tap, res, src, mask, base, smask, sbase, pcol, prow, pxch, slots, nslot, total;
 };
 
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
 
 __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int nrow_max,
-                                                 int nrxl_max, int tmax, int adj_coef, int nsrow_max) {
+                                                 int nrxl_max, int tmax, int adj_coef, int nsrow_max,
+                                                 int slot_cap = 0) {
   TbSmem m;
   const size_t region = size_t(nw) * ky * RX * sizeof(float);
   size_t off = 0;
@@ -209,6 +266,18 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
   m.base = off; off += size_t(nw) * 32 * sizeof(int);
   m.smask = off; off += size_t(nw) * 32 * sizeof(unsigned);
   m.sbase = off; off += size_t(nw) * 32 * sizeof(int);
+  // PML grids (slot_cap > 0): the region's column and row tables (one row more,
+  // for the face above the last band), the double-buffered exchange of each
+  // band's first-row psi_y, and the thread slots (psi_x, psi_y of KY rows)
+  m.pcol = m.prow = m.pxch = m.slots = m.nslot = off;
+  if (slot_cap > 0) {
+    off = tb_align16(off);
+    m.pcol = off; off += size_t(PML_TABLES) * RX * sizeof(float);
+    m.prow = off; off += tb_align16(size_t(PML_TABLES) * (size_t(nw) * ky + 1) * sizeof(float));
+    m.pxch = off; off += size_t(2) * nw * 32 * 16;
+    m.slots = off; off += size_t(slot_cap) * 2 * ky * 16;
+    m.nslot = off; off += 16;
+  }
   m.total = tb_align16(off);
   return m;
 }

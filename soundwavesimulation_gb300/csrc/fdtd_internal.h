@@ -25,8 +25,9 @@ int32_t validate_plain_problem(const fdtd_problem& prob);
 
 // Temporally blocked kernel (fdtd_tb.cu).
 cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st);
-// Sets the dynamic shared-memory attribute of the kernel a launch would use.
-cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem);
+// Sets the dynamic shared-memory attribute of the kernel a launch would use (the
+// PML family for pml).
+cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem, bool pml);
 // One launch over the items of several plans (same rows per lane and warps).
 cudaError_t tb_group_launch(const TbGroup& g, int ky, int nwarps, int mode, int grid, size_t smem,
                             cudaStream_t st);
@@ -55,6 +56,12 @@ struct StepArgs {
   int adjoint;
 };
 cudaError_t step_launch(const StepArgs& a, cudaStream_t st);
+// One step of a PML grid (fdtd_step_pml): tables, dt / 2, dt^2 and the face fields.
+cudaError_t step_pml_launch(const StepArgs& a, const float* pml, float hdt, float dt2, const float* psx,
+                            const float* psy, float* psx_next, float* psy_next, cudaStream_t st);
+// The PML tables of a padded medium, and coef scaled by q = 1 / (1 + a).
+cudaError_t prepare_pml_launch(const double* c, int ny, int nx, int pitch, double dt, double dx, double dy,
+                               int cells, double reflection, float* coef, float* pml, cudaStream_t st);
 cudaError_t gather_launch(int ny, int pitch, int n_shots, const float* fields, int n_rx,
                           const int32_t* rx_rc, const float* rx_w, float* out,
                           long long shot_stride, long long rx_stride, cudaStream_t st);

@@ -99,6 +99,116 @@ __global__ void step_kernel(const StepArgs a) {
   a.u_next[s * plane + (long long)y * P + x] = out;
 }
 
+// One step of a PML grid: cell (y, x) of shot s. The face values on the cell's
+// right and top faces are recomputed from the neighbours' old face fields (the
+// same arithmetic the neighbour does for its own faces), so every value equals
+// the fused kernel's. Beyond the grid u and psi are zero (the rigid wall behind
+// the layer).
+__global__ void step_pml_kernel(const StepArgs a, const float* __restrict__ pml, float hdt, float dt2,
+                                const float* __restrict__ psx, const float* __restrict__ psy, float* psxn,
+                                float* psyn) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int s = blockIdx.z;
+  if (x >= a.nx || y >= a.ny) return;
+  const int ny = a.ny, nx = a.nx, P = a.pitch;
+  const long long plane = (long long)ny * P;
+  const float* u = a.u + s * plane;
+  const float* px = psx + s * plane;
+  const float* py = psy + s * plane;
+  auto U = [&](int yy, int xx) { return (yy < 0 || yy >= ny || xx < 0 || xx >= nx) ? 0.f : u[(long long)yy * P + xx]; };
+  const float* sxc = pml;
+  const float* sxf = pml + nx;
+  const float* axf = pml + 2 * nx;
+  const float* bxf = pml + 3 * nx;
+  const float* syc = pml + PML_TABLES * nx;
+  const float* syf = syc + ny;
+  const float* ayf = syf + ny;
+  const float* byf = ayf + ny;
+  const long long i = (long long)y * P + x;
+  const float uc = U(y, x), ul = U(y, x - 1), ur = U(y, x + 1), ud = U(y - 1, x), uu = U(y + 1, x);
+  const float lap = __fmaf_rn(uc, a.cdiag, nbr4(ul, ur, ud, uu, a.idx2, a.idy2));
+  const float pxl = pml_face(axf[x], px[i], syc[y], sxf[x], bxf[x], __fsub_rn(uc, ul));
+  const float pxr = (x + 1 < nx) ? pml_face(axf[x + 1], px[i + 1], syc[y], sxf[x + 1], bxf[x + 1], __fsub_rn(ur, uc)) : 0.f;
+  const float pyb = pml_face(ayf[y], py[i], sxc[x], syf[y], byf[y], __fsub_rn(uc, ud));
+  const float pyt = (y + 1 < ny) ? pml_face(ayf[y + 1], py[i + P], sxc[x], syf[y + 1], byf[y + 1], __fsub_rn(uu, uc)) : 0.f;
+  float A, M;
+  pml_factors(sxc[x], syc[y], hdt, dt2, A, M);
+  float un = pml_leap(uc, a.u_old[s * plane + i], a.coef[i], A, M, lap, pml_div(pxl, pxr, pyb, pyt));
+  if (a.src_per_shot > 0) {
+    float acc = 0.f;
+    bool hit = false;
+    for (int j = 0; j < a.src_per_shot; ++j) {
+      const int e = s * a.src_per_shot + j;
+      if (a.src_row[e] == y && a.src_col[e] == x && a.src_wave[e] >= 0) {
+        const float v = (a.step < a.wave_len) ? a.waveforms[(long long)a.src_wave[e] * a.wave_len + a.step] : 0.f;
+        acc = inj_acc(acc, a.src_w[e], v);
+        hit = true;
+      }
+    }
+    if (hit) un = inj_add(un, acc);
+  }
+  if (a.dense) {
+    const float d = a.dense[s * plane + i];
+    un = inj_add(un, a.adjoint == 2 ? __fmul_rn(a.coef[i], d) : d);
+  }
+  a.u_next[s * plane + i] = un;
+  psxn[s * plane + i] = pxl;
+  psyn[s * plane + i] = pyb;
+}
+
+// PML tables and the scaled coefficients of a padded medium, in one block: the
+// largest speed (for sigma_max), then per column / row sigma at the centre and at
+// the low face with the face decay and forcing scale, then coef = q (c dt)^2.
+__device__ __forceinline__ double pml_sigma(double xc, int n, int cells, double smax) {
+  const double lo = (cells - 0.5) - xc, hi = xc - (n - cells - 0.5);
+  double d = lo > hi ? lo : hi;
+  if (d < 0.0) d = 0.0;
+  const double r = d / cells;
+  return smax * r * r;
+}
+
+__global__ void pml_prepare_kernel(const double* c, int ny, int nx, int pitch, double dt, double dx, double dy,
+                                   int cells, double reflection, float* coef, float* pml) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (long long i = threadIdx.x; i < (long long)ny * nx; i += blockDim.x) m = fmax(m, c[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = (threadIdx.x < blockDim.x / 32) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) red[0] = m;
+  }
+  __syncthreads();
+  const double cmax = red[0];
+  const double smx = 3.0 * cmax * log(1.0 / reflection) / (2.0 * cells * dx);
+  const double smy = 3.0 * cmax * log(1.0 / reflection) / (2.0 * cells * dy);
+  float* col = pml;
+  float* row = pml + PML_TABLES * nx;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+    const double sc = pml_sigma(i, nx, cells, smx), sf = pml_sigma(i - 0.5, nx, cells, smx);
+    col[i] = (float)sc;
+    col[nx + i] = (float)sf;
+    col[2 * nx + i] = (float)((1.0 - 0.5 * dt * sf) / (1.0 + 0.5 * dt * sf));
+    col[3 * nx + i] = (float)(dt / (dx * dx * (1.0 + 0.5 * dt * sf)));
+  }
+  for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+    const double sc = pml_sigma(j, ny, cells, smy), sf = pml_sigma(j - 0.5, ny, cells, smy);
+    row[j] = (float)sc;
+    row[ny + j] = (float)sf;
+    row[2 * ny + j] = (float)((1.0 - 0.5 * dt * sf) / (1.0 + 0.5 * dt * sf));
+    row[3 * ny + j] = (float)(dt / (dy * dy * (1.0 + 0.5 * dt * sf)));
+  }
+  for (long long k = threadIdx.x; k < (long long)ny * nx; k += blockDim.x) {
+    const int y = (int)(k / nx), x = (int)(k - (long long)y * nx);
+    const double q = 1.0 / (1.0 + 0.5 * dt * (pml_sigma(x, nx, cells, smx) + pml_sigma(y, ny, cells, smy)));
+    const double cd = c[k] * dt;
+    coef[(long long)y * pitch + x] = (float)(cd * cd * q);
+  }
+}
+
 __global__ void gather_kernel(int pitch, long long plane, int n_shots, const float* f, int n_rx,
                               const int32_t* rc, const float* w, float* out,
                               long long shot_stride, long long rx_stride) {
@@ -353,6 +463,20 @@ cudaError_t prepare_medium_launch(const double* c, int ny, int nx, int pitch, do
   if (e != cudaSuccess) return e;
   const int n = (ny > nx ? ny : nx);
   mur_kernel<<<(n + 255) / 256, 256, 0, st>>>(c, ny, nx, dt, dx, dy, mur);
+  return cudaGetLastError();
+}
+
+cudaError_t step_pml_launch(const StepArgs& a, const float* pml, float hdt, float dt2, const float* psx,
+                            const float* psy, float* psx_next, float* psy_next, cudaStream_t st) {
+  dim3 block(32, 8);
+  dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8, a.n_shots);
+  step_pml_kernel<<<grid, block, 0, st>>>(a, pml, hdt, dt2, psx, psy, psx_next, psy_next);
+  return cudaGetLastError();
+}
+
+cudaError_t prepare_pml_launch(const double* c, int ny, int nx, int pitch, double dt, double dx, double dy,
+                               int cells, double reflection, float* coef, float* pml, cudaStream_t st) {
+  pml_prepare_kernel<<<1, 1024, 0, st>>>(c, ny, nx, pitch, dt, dx, dy, cells, reflection, coef, pml);
   return cudaGetLastError();
 }
 

@@ -124,6 +124,12 @@ struct fdtd_plan {
   size_t o_tiles = 0, o_taps = 0, o_rxl = 0, o_recs = 0, o_src = 0, o_stap = 0, o_stap_off = 0;
   size_t o_state[2][2] = {{0, 0}, {0, 0}};
   size_t o_adj[2][2] = {{0, 0}, {0, 0}};
+  // PML grids: the face fields psi_x, psi_y of the forward and adjoint ping-pong
+  // sets and of every checkpoint (float32), and the slots per CTA
+  int pml = 0, slot_cap = 0;
+  size_t o_psi[2][2] = {{0, 0}, {0, 0}};
+  size_t o_apsi[2][2] = {{0, 0}, {0, 0}};
+  size_t o_ckpsi = 0;
   size_t o_ckpt = 0, ckpt_elem_bytes = 4, o_scales = 0, o_seg = 0;
   size_t total = 0;
   size_t smem[3] = {0, 0, 0};
@@ -159,6 +165,8 @@ int32_t fdtd::validate_grid(const fdtd_grid& g) {
   if (g.pitch < g.nx || g.pitch % 4 != 0) return fail(FDTD_ERR_INVALID, "pitch must be a multiple of 4 and >= nx");
   if (!(g.dx > 0) || !(g.dy > 0) || !(g.dt > 0)) return fail(FDTD_ERR_INVALID, "dx, dy and dt must be positive");
   if (!g.coef || !g.mur) return fail(FDTD_ERR_INVALID, "coef and mur must be set");
+  if (g.pml && (g.pml_cells < 1 || 2 * g.pml_cells >= std::min(g.nx, g.ny)))
+    return fail(FDTD_ERR_INVALID, "PML layer must be at least 1 cell and thinner than half the grid");
   return FDTD_OK;
 }
 
@@ -226,6 +234,12 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.nrx = p->prob.rx.n;
   q.nt = p->prob.n_steps;
   q.seg_stride = (long long)p->field_elems;
+  if (p->pml) {
+    q.pml = g.pml;
+    q.hdt = (float)(0.5 * g.dt);
+    q.dt2 = (float)(g.dt * g.dt);
+    q.slot_cap = p->slot_cap;
+  }
 }
 
 int grid_size(const fdtd_plan* p) {
@@ -247,6 +261,8 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
   const fdtd_grid& g = prob->grid;
   const int ny = g.ny, nx = g.nx, KY = p->ky, RY = p->RY;
   const int halo = p->tmax + 1;
+  p->pml = g.pml ? g.pml_cells : 0;
+  p->slot_cap = 0;
   std::vector<AxisTile> tx, ty;
   std::string err = tile_axis(nx, RX, 4, halo, 0, tx);
   if (!err.empty()) return fail(FDTD_ERR_UNSUPPORTED, "x tiling: " + err);
@@ -305,6 +321,25 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
                 ((ay.flags & 1) ? TF_BOTTOM : 0) | ((ay.flags & 2) ? TF_TOP : 0) |
                 (((ax.flags | ay.flags) & 4) ? TF_OUTSIDE : 0);
       if ((t.flags & TF_LEFT) && t.rx0 != 0) return fail(FDTD_ERR_UNSUPPORTED, "left edge tile must start at column 0");
+      if (g.pml) {
+        // no Mur edges; a region holding layer cells is a PML tile, and each of its
+        // threads whose columns or rows enter the layer takes a slot
+        t.flags &= ~TF_MUR;
+        const int P = g.pml_cells;
+        auto in_layer = [](int v, int n, int P) { return v >= 0 && v < n && (v < P || v >= n - P); };
+        int slots = 0;
+        for (int w = 0; w < p->nw; ++w) {
+          bool rows = false;
+          for (int r = 0; r < KY; ++r) rows = rows || in_layer(t.ry0 + w * KY + r, ny, P);
+          for (int l = 0; l < 32; ++l) {
+            bool cols = false;
+            for (int c = 0; c < 4; ++c) cols = cols || in_layer(t.rx0 + 4 * l + c, nx, P);
+            if (rows || cols) ++slots;
+          }
+        }
+        if (slots > 0) t.flags |= TF_PML;
+        p->slot_cap = std::max(p->slot_cap, slots);
+      }
       // taps inside the region, sorted by (thread, bit)
       std::vector<std::pair<int, int>> local;  // (packed, node id)
       for (size_t id = 0; id < nodes.size(); ++id) {
@@ -518,6 +553,63 @@ int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pit
   return FDTD_OK;
 }
 
+int32_t fdtd_prepare_medium_pml(const double* c, int32_t ny, int32_t nx, int32_t pitch, double dt, double dx,
+                                double dy, int32_t cells, double reflection, float* coef, float* mur, float* pml,
+                                void* stream) {
+  if (!c || !coef || !mur || !pml) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (ny < 8 || nx < 8 || pitch < nx || pitch % 4) return fail(FDTD_ERR_INVALID, "bad grid shape");
+  if (!(dt > 0) || !(dx > 0) || !(dy > 0)) return fail(FDTD_ERR_INVALID, "dx, dy and dt must be positive");
+  if (cells < 1 || 2 * cells >= std::min(nx, ny)) return fail(FDTD_ERR_INVALID, "bad PML thickness");
+  if (!(reflection > 0 && reflection < 1)) return fail(FDTD_ERR_INVALID, "reflection must lie in (0, 1)");
+  cudaError_t e = prepare_medium_launch(c, ny, nx, pitch, dt, dx, dy, coef, mur, (cudaStream_t)stream);
+  if (e == cudaSuccess)
+    e = prepare_pml_launch(c, ny, nx, pitch, dt, dx, dy, cells, reflection, coef, pml, (cudaStream_t)stream);
+  return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "prepare_medium_pml");
+}
+
+int32_t fdtd_step_pml(const fdtd_grid* grid, int32_t n_shots, const float* u_old, const float* u, float* u_next,
+                      const float* psx, const float* psy, float* psx_next, float* psy_next, int32_t src_per_shot,
+                      const int32_t* src_row, const int32_t* src_col, const float* src_w, const int32_t* src_wave,
+                      const float* waveforms, int32_t waveform_len, int32_t step, const float* dense,
+                      int32_t adjoint, void* stream) {
+  if (!grid) return fail(FDTD_ERR_INVALID, "null grid");
+  int32_t rc = validate_grid(*grid);
+  if (rc) return rc;
+  if (!grid->pml) return fail(FDTD_ERR_INVALID, "fdtd_step_pml needs a grid with PML tables");
+  if (n_shots < 1 || !u_old || !u || !u_next || !psx || !psy || !psx_next || !psy_next)
+    return fail(FDTD_ERR_INVALID, "null field");
+  if (adjoint != 0 && adjoint != 2) return fail(FDTD_ERR_INVALID, "adjoint must be 0 or 2 on a PML grid");
+  if (src_per_shot > 0 && (!src_row || !src_col || !src_w || !src_wave || !waveforms))
+    return fail(FDTD_ERR_INVALID, "source arrays missing");
+  StepArgs a;
+  a.ny = grid->ny;
+  a.nx = grid->nx;
+  a.pitch = grid->pitch;
+  const double idx2 = 1.0 / (grid->dx * grid->dx), idy2 = 1.0 / (grid->dy * grid->dy);
+  a.idx2 = (float)idx2;
+  a.idy2 = (float)idy2;
+  a.cdiag = (float)(-2.0 * (idx2 + idy2));
+  a.coef = grid->coef;
+  a.mur = grid->mur;
+  a.n_shots = n_shots;
+  a.u_old = u_old;
+  a.u = u;
+  a.u_next = u_next;
+  a.src_per_shot = src_per_shot > 0 ? src_per_shot : 0;
+  a.src_row = src_row;
+  a.src_col = src_col;
+  a.src_w = src_w;
+  a.src_wave = src_wave;
+  a.waveforms = waveforms;
+  a.wave_len = waveform_len;
+  a.step = step;
+  a.dense = dense;
+  a.adjoint = adjoint;
+  cudaError_t e = step_pml_launch(a, grid->pml, (float)(0.5 * grid->dt), (float)(grid->dt * grid->dt), psx, psy,
+                                  psx_next, psy_next, (cudaStream_t)stream);
+  return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "fdtd_step_pml");
+}
+
 int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, const float* u,
                   float* u_next, int32_t src_per_shot, const int32_t* src_row,
                   const int32_t* src_col, const float* src_w, const int32_t* src_wave,
@@ -679,9 +771,11 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   rc = build_tables(p, problem);
   if (rc) { delete p; return rc; }
   // the adjoint keeps its coefficient tile in shared memory when that fits
-  p->adj_coef = tb_smem_layout(p->nw, p->ky, MODE_ADJ, p->nrow_max, p->nrxl_max, p->tmax, 1, p->nsrow_max).total <= SMEM_LIMIT;
+  p->adj_coef = tb_smem_layout(p->nw, p->ky, MODE_ADJ, p->nrow_max, p->nrxl_max, p->tmax, 1, p->nsrow_max,
+                               p->slot_cap).total <= SMEM_LIMIT;
   for (int m = 0; m < 3; ++m) {
-    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->nrow_max, p->nrxl_max, p->tmax, p->adj_coef, p->nsrow_max).total;
+    p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->nrow_max, p->nrxl_max, p->tmax, p->adj_coef, p->nsrow_max,
+                                p->slot_cap).total;
     if (p->smem[m] > SMEM_LIMIT && (m == MODE_FWD || for_gradient)) {
       delete p;
       return fail(FDTD_ERR_UNSUPPORTED, "shared memory need exceeds 227 KB; use fewer steps per launch or warps");
@@ -701,9 +795,18 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   p->o_stap_off = off; off = align_up(off + p->stap_off.size() * sizeof(int));
   for (int s = 0; s < 2; ++s)
     for (int f = 0; f < 2; ++f) { p->o_state[s][f] = off; off = align_up(off + fb); }
+  if (p->pml)
+    for (int s = 0; s < 2; ++s)
+      for (int f = 0; f < 2; ++f) { p->o_psi[s][f] = off; off = align_up(off + fb); }
   if (p->for_gradient) {
     for (int s = 0; s < 2; ++s)
       for (int f = 0; f < 2; ++f) { p->o_adj[s][f] = off; off = align_up(off + fb); }
+    if (p->pml) {
+      for (int s = 0; s < 2; ++s)
+        for (int f = 0; f < 2; ++f) { p->o_apsi[s][f] = off; off = align_up(off + fb); }
+      p->o_ckpsi = off;  // checkpoints 1..nseg-1, psi_x and psi_y each (float32)
+      off = align_up(off + (size_t)(p->nseg - 1) * 2 * fb);
+    }
     p->ckpt_elem_bytes = (t.ckpt_store == FDTD_STORE_F32) ? 4 : 2;
     const size_t nck = (size_t)(p->nseg - 1) * 2;  // checkpoints 1..nseg-1, two fields each
     p->o_ckpt = off; off = align_up(off + nck * p->field_elems * p->ckpt_elem_bytes);
@@ -759,6 +862,23 @@ int32_t fdtd_plan_bind(fdtd_plan* p, void* workspace, size_t bytes, void* stream
     e = cudaMemcpyAsync(p->ws + u.off, u.src, u.n, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "table upload");
   }
+  if (p->pml) {
+    // PML face fields start at zero and stay zero outside the PML tiles, which
+    // never write there
+    const size_t fb = p->field_elems * sizeof(float);
+    std::vector<std::pair<size_t, size_t>> zero;
+    for (int a = 0; a < 2; ++a)
+      for (int f = 0; f < 2; ++f) {
+        zero.push_back({p->o_psi[a][f], fb});
+        if (p->for_gradient) zero.push_back({p->o_apsi[a][f], fb});
+      }
+    if (p->for_gradient) zero.push_back({p->o_ckpsi, (size_t)(p->nseg - 1) * 2 * fb});
+    for (const auto& z : zero) {
+      if (!z.second) continue;
+      e = cudaMemsetAsync(p->ws + z.first, 0, z.second, st);
+      if (e != cudaSuccess) return cuda_fail(e, "PML field clear");
+    }
+  }
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, "table upload sync");
   p->bound = true;
@@ -797,7 +917,7 @@ int32_t run_graphed(fdtd_plan* p, fdtd_plan::Graph& g, const void* const (&key)[
     if (e != cudaSuccess) return cuda_fail(e, "capture stream");
     // kernel attributes are set outside the capture
     for (int m = 0; m < 3; ++m) {
-      e = tb_configure(p->ky, m, p->nw, p->smem[m]);
+      e = tb_configure(p->ky, m, p->nw, p->smem[m], p->pml != 0);
       if (e != cudaSuccess) return cuda_fail(e, "kernel attributes");
     }
     e = cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal);
@@ -915,6 +1035,8 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
   const size_t fb = p->field_elems * sizeof(float);
   int32_t rc0 = k.memset(p->ws + p->o_state[0][0], fb);
   if (!rc0) rc0 = k.memset(p->ws + p->o_state[0][1], fb);
+  if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_psi[0][0], fb);
+  if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_psi[0][1], fb);
   if (rc0) return rc0;
   TbParams q;
   fill_params(p, q);
@@ -923,6 +1045,10 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
   const float* in_prev = fptr(p, p->o_state[0][0]);
   const float* in_cur = fptr(p, p->o_state[0][1]);
   int in_set = 0;  // 0/1 = ping-pong set, -1 = elsewhere
+  // PML face fields: their own ping-pong, written to the checkpoints at segment ends
+  const float* in_px = p->pml ? fptr(p, p->o_psi[0][0]) : nullptr;
+  const float* in_py = p->pml ? fptr(p, p->o_psi[0][1]) : nullptr;
+  int psi_set = 0;
   for (int n0 = 0; n0 < nt; n0 += T) {
     const int ns = std::min(T, nt - n0), end = n0 + ns;
     const int out_set = (in_set == 0) ? 1 : 0;
@@ -947,6 +1073,22 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
     q.out_cur = out_cur;
     q.n0 = n0;
     q.nsteps = ns;
+    if (p->pml) {
+      const int ps_out = (psi_set == 0) ? 1 : 0;
+      q.in_psx = in_px;
+      q.in_psy = in_py;
+      if (ckpt) {
+        q.out_psx = fptr(p, p->o_ckpsi + (size_t)(j - 1) * 2 * fb);
+        q.out_psy = fptr(p, p->o_ckpsi + ((size_t)(j - 1) * 2 + 1) * fb);
+        psi_set = -1;
+      } else {
+        q.out_psx = fptr(p, p->o_psi[ps_out][0]);
+        q.out_psy = fptr(p, p->o_psi[ps_out][1]);
+        psi_set = ps_out;
+      }
+      in_px = q.out_psx;
+      in_py = q.out_psy;
+    }
     int32_t rc = k.launch_tb(MODE_FWD, q);
     if (rc) return rc;
     if (ckpt && p->tun.ckpt_store != FDTD_STORE_F32) {
@@ -971,6 +1113,8 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Si
   const size_t fb = p->field_elems * sizeof(float);
   int32_t rc0 = k.memset(p->ws + p->o_adj[0][0], fb);
   if (!rc0) rc0 = k.memset(p->ws + p->o_adj[0][1], fb);
+  if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_apsi[0][0], fb);
+  if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_apsi[0][1], fb);
   if (rc0) return rc0;
   TbParams q;
   fill_params(p, q);
@@ -986,6 +1130,23 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Si
     const float* in_prev;
     const float* in_cur;
     int in_set;
+    // the forward's PML face fields at the segment start
+    const float* in_px = nullptr;
+    const float* in_py = nullptr;
+    int psi_set = 0;
+    if (p->pml) {
+      if (j == 0) {
+        int32_t rc = k.memset(p->ws + p->o_psi[0][0], fb);
+        if (!rc) rc = k.memset(p->ws + p->o_psi[0][1], fb);
+        if (rc) return rc;
+        in_px = fptr(p, p->o_psi[0][0]);
+        in_py = fptr(p, p->o_psi[0][1]);
+      } else {
+        in_px = fptr(p, p->o_ckpsi + (size_t)(j - 1) * 2 * fb);
+        in_py = fptr(p, p->o_ckpsi + ((size_t)(j - 1) * 2 + 1) * fb);
+        psi_set = -1;
+      }
+    }
     if (j == 0) {
       int32_t rc = k.memset(p->ws + p->o_state[0][0], fb);
       if (!rc) rc = k.memset(p->ws + p->o_state[0][1], fb);
@@ -1023,6 +1184,16 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Si
       q.out_cur = fptr(p, p->o_state[out_set][1]);
       q.n0 = n0;
       q.nsteps = ns;
+      if (p->pml) {
+        const int ps_out = (psi_set == 0) ? 1 : 0;
+        q.in_psx = in_px;
+        q.in_psy = in_py;
+        q.out_psx = fptr(p, p->o_psi[ps_out][0]);
+        q.out_psy = fptr(p, p->o_psi[ps_out][1]);
+        in_px = q.out_psx;
+        in_py = q.out_psy;
+        psi_set = ps_out;
+      }
       int32_t rc = k.launch_tb(MODE_REC, q);
       if (rc) return rc;
       in_prev = q.out_prev;
@@ -1039,6 +1210,12 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Si
       q.out_cur = fptr(p, p->o_adj[out][1]);
       q.n0 = ntop;
       q.nsteps = ns;
+      if (p->pml) {  // the adjoint's own face fields (the same PML acts on w)
+        q.in_psx = fptr(p, p->o_apsi[adj_in][0]);
+        q.in_psy = fptr(p, p->o_apsi[adj_in][1]);
+        q.out_psx = fptr(p, p->o_apsi[out][0]);
+        q.out_psy = fptr(p, p->o_apsi[out][1]);
+      }
       int32_t rc = k.launch_tb(MODE_ADJ, q);
       if (rc) return rc;
       adj_in = out;
@@ -1080,6 +1257,7 @@ int32_t group_run(fdtd_plan* const* plans, int n, void* workspace, size_t bytes,
     if (!plans[i] || !plans[i]->bound) return fail(FDTD_ERR_STATE, "group: every plan must be bound");
     if (plans[i]->ky != plans[0]->ky || plans[i]->nw != plans[0]->nw)
       return fail(FDTD_ERR_UNSUPPORTED, "group: plans must share rows_per_lane and warps");
+    if (plans[i]->pml) return fail(FDTD_ERR_UNSUPPORTED, "group: grids with a PML layer run as separate plans");
   }
   if (!workspace || bytes < group_bytes(plans, n)) return fail(FDTD_ERR_WORKSPACE, "group: workspace too small");
   // every plan's pass as a list of operations
