@@ -173,6 +173,9 @@ int32_t fdtd::validate_grid(const fdtd_grid& g) {
 int32_t fdtd::validate_plain_problem(const fdtd_problem& prob) {
   int32_t rc = validate_grid(prob.grid);
   if (rc) return rc;
+  if (prob.grid.pml)
+    return fail(FDTD_ERR_UNSUPPORTED, "the plain per-shot forms run grids with Mur edges; a PML grid runs in the "
+                                      "fused engine or with fdtd_step_pml");
   const fdtd_grid& g = prob.grid;
   if (prob.n_shots < 1 || prob.n_steps < 1) return fail(FDTD_ERR_INVALID, "n_shots and n_steps must be positive");
   const int R = prob.rx.n;
@@ -619,6 +622,7 @@ int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, co
   if (grid->ny < 3 || grid->nx < 3 || grid->pitch < grid->nx || grid->pitch % 4)
     return fail(FDTD_ERR_INVALID, "bad grid shape");
   if (!grid->coef || !grid->mur || !u_old || !u || !u_next) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (grid->pml) return fail(FDTD_ERR_INVALID, "a PML grid steps with fdtd_step_pml");
   if (u_next == u || u_next == u_old) return fail(FDTD_ERR_INVALID, "u_next must not alias the inputs");
   if (n_shots < 1) return fail(FDTD_ERR_INVALID, "n_shots must be positive");
   if (src_per_shot > 0 && (!src_row || !src_col || !src_w || !src_wave || !waveforms))

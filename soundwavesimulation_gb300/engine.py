@@ -46,26 +46,50 @@ def ptr(t) -> int:
 
 
 class DeviceMedium:
-    """Float32 coefficients (c dt)^2 and Mur edge coefficients of one grid."""
+    """Float32 coefficients (c dt)^2 and Mur edge coefficients of one grid.
 
-    def __init__(self, c, dx, dy, dt, device):
+    With ``pml_cells`` > 0 the grid is padded by a PML layer of that many cells on
+    every side (the medium extended with its edge values), which replaces the Mur
+    edges; ``pml_reflection`` sets the damping profile's target reflection. The
+    physical grid is then rows / columns ``[pml_cells, pml_cells + n)`` of the
+    padded one: ``ny``, ``nx`` are the padded sizes, ``phys_shape`` the physical
+    ones, and receivers / sources given on the physical grid are shifted by
+    ``pml_cells`` (ProblemTables does that).
+    """
+
+    def __init__(self, c, dx, dy, dt, device, pml_cells=0, pml_reflection=1e-5):
         self.device = require_cuda(device)
         c64 = torch.as_tensor(c, dtype=torch.float64).to(self.device).contiguous()
         if c64.ndim != 2:
             raise ValueError("Sound speed c must be a 2D array (ny, nx).")
-        self.ny, self.nx = (int(s) for s in c64.shape)
+        self.pml_cells = int(pml_cells)
+        self.pml_reflection = float(pml_reflection)
+        if self.pml_cells < 0:
+            raise ValueError("pml_cells must not be negative.")
+        self.phys_shape = tuple(int(s) for s in c64.shape)
+        P = self.pml_cells
+        self.ny, self.nx = self.phys_shape[0] + 2 * P, self.phys_shape[1] + 2 * P
         self.pitch = padded_width(self.nx)
         self.dx, self.dy, self.dt = float(dx), float(dy), float(dt)
-        self.c64 = c64
+        self.c64 = torch.empty((self.ny, self.nx), dtype=torch.float64, device=self.device)
         self.coef = torch.zeros((self.ny, self.pitch), dtype=torch.float32, device=self.device)
         self.mur = torch.zeros(2 * (2 * self.ny + 2 * self.nx + 8), dtype=torch.float32, device=self.device)
+        self.pml = (torch.zeros(4 * (self.nx + self.ny), dtype=torch.float32, device=self.device)
+                    if P else None)
+        self._load(c64)
         self.prepare()
+
+    def _load(self, c64):
+        P = self.pml_cells
+        if P:
+            c64 = torch.nn.functional.pad(c64[None, None], (P, P, P, P), mode="replicate")[0, 0]
+        self.c64.copy_(c64)
 
     def set_c(self, c):
         c64 = torch.as_tensor(c, dtype=torch.float64).to(self.device)
-        if tuple(c64.shape) != (self.ny, self.nx):
-            raise ValueError(f"Sound speed shape {tuple(c64.shape)} does not match {(self.ny, self.nx)}.")
-        self.c64.copy_(c64)
+        if tuple(c64.shape) != self.phys_shape:
+            raise ValueError(f"Sound speed shape {tuple(c64.shape)} does not match {self.phys_shape}.")
+        self._load(c64)
         self.prepare()
 
     def set_dt(self, dt):
@@ -74,13 +98,24 @@ class DeviceMedium:
 
     def prepare(self):
         lib = _lib.load()
+        if self.pml_cells:
+            _lib.check(lib.fdtd_prepare_medium_pml(ptr(self.c64), self.ny, self.nx, self.pitch, self.dt, self.dx,
+                                                   self.dy, self.pml_cells, self.pml_reflection, ptr(self.coef),
+                                                   ptr(self.mur), ptr(self.pml), stream_handle(self.device)),
+                       "prepare_medium_pml")
+            return
         _lib.check(lib.fdtd_prepare_medium(ptr(self.c64), self.ny, self.nx, self.pitch, self.dt,
                                            self.dx, self.dy, ptr(self.coef), ptr(self.mur),
                                            stream_handle(self.device)), "prepare_medium")
 
     def grid(self) -> _lib.Grid:
         return _lib.Grid(self.ny, self.nx, self.pitch, self.dx, self.dy, self.dt,
-                         ptr(self.coef), ptr(self.mur))
+                         ptr(self.coef), ptr(self.mur), ptr(self.pml), self.pml_cells)
+
+    def physical(self, field):
+        """The physical-grid view of a padded (..., ny, pitch) field."""
+        P = self.pml_cells
+        return field[..., P:P + self.phys_shape[0], P:P + self.phys_shape[1]]
 
     def new_field(self, n_shots=None):
         shape = (self.ny, self.pitch) if n_shots is None else (int(n_shots), self.ny, self.pitch)
@@ -97,12 +132,13 @@ class ProblemTables:
     def __init__(self, medium: DeviceMedium, receivers, sources, waveforms: torch.Tensor, n_steps: int):
         self.medium = medium
         row0, col0, w = receivers
-        self._rx_row0 = np.ascontiguousarray(row0, dtype=np.int32)
-        self._rx_col0 = np.ascontiguousarray(col0, dtype=np.int32)
+        P = medium.pml_cells  # physical-grid indices into the padded grid
+        self._rx_row0 = np.ascontiguousarray(np.asarray(row0) + P, dtype=np.int32)
+        self._rx_col0 = np.ascontiguousarray(np.asarray(col0) + P, dtype=np.int32)
         self._rx_w = np.ascontiguousarray(w, dtype=np.float32).reshape(-1, 4)
         rows, cols, sw, wave = (np.ascontiguousarray(a) for a in sources)
-        self._s_row = rows.astype(np.int32).reshape(rows.shape[0], -1)
-        self._s_col = cols.astype(np.int32).reshape(self._s_row.shape)
+        self._s_row = (rows.astype(np.int64) + P).astype(np.int32).reshape(rows.shape[0], -1)
+        self._s_col = (cols.astype(np.int64) + P).astype(np.int32).reshape(self._s_row.shape)
         self._s_w = sw.astype(np.float32).reshape(self._s_row.shape)
         self._s_wave = wave.astype(np.int32).reshape(self._s_row.shape)
         if waveforms.dtype != torch.float32 or waveforms.device != medium.device or waveforms.ndim != 2:

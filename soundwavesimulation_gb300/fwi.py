@@ -277,7 +277,7 @@ class TorchLeastSquaresFWI:
             residual, _ = residual_misfit(predicted, observed, self._mute(shot_batch), residual=predicted,
                                           misfit=total)
             plan.adjoint(residual, g_c2)
-        g_m = chain_rule(g_c2[:, :medium.nx].contiguous(), m, self._mask_dev)
+        g_m = chain_rule(medium.physical(g_c2).contiguous(), m, self._mask_dev)
         regularization_device(m, self._mask_u8, self.alpha, self.tv, self.tv_eps, g_m, total)
         return float(total.item()), g_m
 
@@ -297,7 +297,7 @@ class TorchLeastSquaresFWI:
             residual, _ = residual_misfit(predicted, observed, self._mute(shot_batch), residual=predicted,
                                           misfit=total)
             plan.adjoint(residual, g_c2)
-        return float(total.item()), g_c2[:, :medium.nx].cpu().numpy()
+        return float(total.item()), medium.physical(g_c2).cpu().numpy()
 
 
 class ArcLeastSquaresFWI(TorchLeastSquaresFWI):
@@ -341,7 +341,7 @@ class WaveformMisfit(torch.autograd.Function):
         medium = plan.medium
         g_c2 = torch.zeros((medium.ny, medium.pitch), dtype=torch.float64, device=medium.device)
         plan.adjoint(grad_traces.detach().to(torch.float32).contiguous(), g_c2)
-        g_m = chain_rule(g_c2[:, :medium.nx].contiguous(), m64.to(medium.device), None)
+        g_m = chain_rule(medium.physical(g_c2).contiguous(), m64.to(medium.device), None)
         return g_m.to(device=ctx.m_device, dtype=ctx.m_dtype), None, None
 
 

@@ -174,34 +174,59 @@ class TorchScalarWave2D:
 
 
 class _Rotation:
-    """Three padded field buffers rotated u_old <- u <- u_next."""
+    """Three padded field buffers rotated u_old <- u <- u_next (and, on a PML grid,
+    two sets of face fields psi_x, psi_y swapped every step)."""
 
     def __init__(self, medium: DeviceMedium, n_shots=None):
-        self.nx = medium.nx
+        self.medium = medium
         shape = (3,) + ((medium.ny, medium.pitch) if n_shots is None else (n_shots, medium.ny, medium.pitch))
         self.buf = torch.zeros(shape, dtype=torch.float32, device=medium.device)
         self.io, self.ic, self.inx = 0, 1, 2
+        self.psi = (torch.zeros((2, 2) + shape[1:], dtype=torch.float32, device=medium.device)
+                    if medium.pml_cells else None)
+        self.ps = 0
 
     def rotate(self):
         self.io, self.ic, self.inx = self.ic, self.inx, self.io
+        self.ps ^= 1
 
     def view(self, i):
-        return self.buf[i][..., :self.nx]
+        return self.medium.physical(self.buf[i])
 
     def zero(self):
         self.buf.zero_()
+        if self.psi is not None:
+            self.psi.zero_()
+
+    def step(self, lib, grid, n_shots, n_src, rows, cols, w, wave, value, dense, adjoint, stream):
+        """One leapfrog step of the rotation's fields through the C ABI."""
+        if self.psi is None:
+            return lib.fdtd_step(ctypes.byref(grid), n_shots, ptr(self.buf[self.io]), ptr(self.buf[self.ic]),
+                                 ptr(self.buf[self.inx]), n_src, ptr(rows), ptr(cols), ptr(w), ptr(wave),
+                                 ptr(value), 1, 0, ptr(dense), int(adjoint), stream)
+        if adjoint == 1:
+            raise ValueError("a PML grid carries the adjoint as w = (c dt)^2 l (adjoint=2)")
+        a, b = self.psi[self.ps], self.psi[self.ps ^ 1]
+        return lib.fdtd_step_pml(ctypes.byref(grid), n_shots, ptr(self.buf[self.io]), ptr(self.buf[self.ic]),
+                                 ptr(self.buf[self.inx]), ptr(a[0]), ptr(a[1]), ptr(b[0]), ptr(b[1]), n_src,
+                                 ptr(rows), ptr(cols), ptr(w), ptr(wave), ptr(value), 1, 0, ptr(dense),
+                                 int(adjoint), stream)
 
 
 class TorchFDTD2D:
     """Single-shot leapfrog solver with Mur edges (fdtd2d/torch_backend.py:236-344)."""
 
-    def __init__(self, model: TorchScalarWave2D, dt: float, compile_step=False):
+    def __init__(self, model: TorchScalarWave2D, dt: float, compile_step=False, pml_cells=0, pml_reflection=1e-5):
+        """``pml_cells`` > 0 replaces the Mur edges by a PML layer of that many cells
+        padded outside the grid (an extension; the reference has Mur edges only).
+        Fields, sources and receivers stay on the physical grid."""
         self.model = model
         self.dt = float(dt)
         self.dt2 = self.dt * self.dt
         if self.cfl >= 1.0:
             raise ValueError(f"Unstable time step: CFL = {self.cfl:.3f} >= 1.")
-        self.medium = DeviceMedium(model._c64, model.dx, model.dy, self.dt, model.device)
+        self.medium = DeviceMedium(model._c64, model.dx, model.dy, self.dt, model.device, pml_cells=pml_cells,
+                                   pml_reflection=pml_reflection)
         self._version = model.version
         self._rot = _Rotation(self.medium)
         self._dense = self.medium.new_field()
@@ -234,7 +259,8 @@ class TorchFDTD2D:
     def set_source(self, row: int, col: int):
         self.source_row = int(row)
         self.source_col = int(col)
-        self._src.copy_(torch.tensor([self.source_row, self.source_col], dtype=torch.int32))
+        P = self.medium.pml_cells
+        self._src.copy_(torch.tensor([self.source_row + P, self.source_col + P], dtype=torch.int32))
 
     def set_c(self, c):
         self.model.set_c(c)
@@ -258,13 +284,14 @@ class TorchFDTD2D:
                 self._value.fill_(float(value))
             n_src = 1
         elif source_mode == 2:
-            self._dense[:, :self.medium.nx].copy_(torch.as_tensor(source_field, device=self.model.device))
+            self.medium.physical(self._dense).copy_(torch.as_tensor(source_field, device=self.model.device))
             dense = self._dense
         r = self._rot
-        _lib.check(lib.fdtd_step(ctypes.byref(grid), 1, ptr(r.buf[r.io]), ptr(r.buf[r.ic]), ptr(r.buf[r.inx]),
-                                 n_src, ptr(self._src), ptr(self._src[1:]), ptr(self._src_w),
-                                 ptr(self._src_wave), ptr(self._value), 1, 0, ptr(dense), int(bool(adjoint)),
-                                 stream_handle(self.model.device)), "step")
+        if adjoint and self.medium.pml_cells:
+            raise ValueError("the per-step adjoint runs on Mur grids; a PML grid's adjoint runs in the fused "
+                             "gradient (TorchLeastSquaresFWI, fwi.WaveformMisfit)")
+        _lib.check(r.step(lib, grid, 1, n_src, self._src, self._src[1:], self._src_w, self._src_wave, self._value,
+                          dense, int(bool(adjoint)), stream_handle(self.model.device)), "step")
         r.rotate()
         return self.u
 
@@ -521,8 +548,9 @@ class TorchFDTD2DBatch:
         self._rows_h, self._cols_h = rows_h, cols_h
         self.source_rows.copy_(torch.as_tensor(rows_h))
         self.source_cols.copy_(torch.as_tensor(cols_h))
-        self._src_row.copy_(torch.as_tensor(rows_h, dtype=torch.int32))
-        self._src_col.copy_(torch.as_tensor(cols_h, dtype=torch.int32))
+        P = self._solver.medium.pml_cells
+        self._src_row.copy_(torch.as_tensor(rows_h + P, dtype=torch.int32))
+        self._src_col.copy_(torch.as_tensor(cols_h + P, dtype=torch.int32))
 
     def _launch(self, value=None, dense=None, adjoint=False):
         self._solver._sync_medium()
@@ -535,10 +563,11 @@ class TorchFDTD2DBatch:
             n_src = 1
         r = self._rot
         grid = self._solver.medium.grid()
-        _lib.check(_lib.load().fdtd_step(ctypes.byref(grid), self.n_shots, ptr(r.buf[r.io]), ptr(r.buf[r.ic]),
-                                         ptr(r.buf[r.inx]), n_src, ptr(self._src_row), ptr(self._src_col),
-                                         ptr(self._src_w), ptr(self._src_wave), ptr(self._value), 1, 0,
-                                         ptr(dense), int(bool(adjoint)), stream_handle(self.model.device)),
+        if adjoint and self._solver.medium.pml_cells:
+            raise ValueError("the per-step adjoint runs on Mur grids; a PML grid's adjoint runs in the fused "
+                             "gradient (TorchLeastSquaresFWI, fwi.WaveformMisfit)")
+        _lib.check(r.step(_lib.load(), grid, self.n_shots, n_src, self._src_row, self._src_col, self._src_w,
+                          self._src_wave, self._value, dense, int(bool(adjoint)), stream_handle(self.model.device)),
                    "step")
         r.rotate()
         return self.u
