@@ -1065,6 +1065,9 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
             x.slot[r] = a;
             x.slot[KY + r] = b;
           }
+          // the first step's old psi_y of this band's first row, for the band below
+          // (the exchange buffer the first step reads; a barrier follows)
+          x.s_pxch[x.w * 32 + x.lane] = x.slot[KY];
         }
       }
     }

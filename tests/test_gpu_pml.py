@@ -64,7 +64,7 @@ def _plan(engine, medium, p, tuning=None, for_gradient=False, truth=False):
     (150, 133, 20, {"rows_per_lane": 8, "warps": 16, "steps_per_launch": 12}),
     (171, 260, 30, {"rows_per_lane": 4, "warps": 16, "steps_per_launch": 9}),
     (200, 141, 12, {"rows_per_lane": 8, "warps": 12, "steps_per_launch": 15}),
-    (129, 300, 25, {"rows_per_lane": 4, "warps": 32, "steps_per_launch": 7}),
+    (129, 300, 25, {"rows_per_lane": 4, "warps": 16, "steps_per_launch": 7}),
 ])
 def test_fused_pml_traces_vs_float64_and_one_step_kernel(eng, ny, nx, P, tuning):
     _lib, engine = eng
@@ -99,7 +99,7 @@ def test_fused_pml_traces_vs_float64_and_one_step_kernel(eng, ny, nx, P, tuning)
                                    rw.data_ptr(), out[:, :, n:].data_ptr(), out.stride(0), out.stride(1), stream),
                    "gather")
         io, ic, inx, ps = ic, inx, io, ps ^ 1
-    assert torch.equal(out, traces)
+    assert torch.equal(out, traces), float((out - traces).abs().max())
 
 
 def test_pml_gradient_vs_float64(eng):
