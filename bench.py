@@ -357,6 +357,39 @@ def bench_gradient(args, acq, medium, rx, waves, observed, tuning, device, world
     }
 
 
+def bench_pml(args, acq, waves, traces, device, barrier, cells=30):
+    """The same forward with a PML of ``cells`` cells padded outside the grid (the
+    layer the configuration names) instead of Mur edges: throughput in physical
+    cell-updates/s and in computed (padded-grid) ones, and the trace change the
+    layer makes against the Mur run (the Mur echoes it removes)."""
+    import torch
+    from soundwavesimulation_gb300.autotune import autotune
+    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan
+    medium = DeviceMedium(acq.c, acq.dx, acq.dx, acq.dt, device, pml_cells=cells)
+    rx = acq.ring.receiver_taps()
+    tuning = autotune(medium, rx, acq.source_tables(), waves, acq.n_steps)
+    plan = FusedPlan(medium, rx, acq.source_tables(), waves, acq.n_steps, tuning=tuning)
+    out = torch.empty_like(traces)
+    for _ in range(args.warmup):
+        plan.forward(out)
+    barrier()
+    stream = torch.cuda.current_stream()
+    steps = max(1, min(args.steps, 5))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record(stream)
+    for k in range(steps):
+        plan.forward(out)
+        ev[k + 1].record(stream)
+    barrier()
+    ms = float(np.mean([ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]))
+    padded = float(medium.ny) * medium.nx * acq.n_shots * acq.n_steps
+    change = float(torch.linalg.vector_norm(out - traces) / torch.linalg.vector_norm(traces))
+    return {"cells": cells, "value": acq.cell_updates / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms,
+            "computed_value": padded / (ms * 1e-3) / 1e9, "grid": [medium.ny, medium.nx], "tuning": plan.tuning,
+            "trace_change_vs_mur": change,
+            "note": "value counts physical cell-updates (512^2 per shot-step); computed_value the padded grid's"}
+
+
 def _full_gather(traces, acq):
     """(n_elements, R, nt) observed gathers with the bench's shots at their transmitter rows."""
     import torch
@@ -464,6 +497,9 @@ def run_ours(args):
     h2d = acq.c.size * 8 + nt * 4 + 2 * S * 8
     d2h = int(host_traces.numel()) * 4
 
+    # ---- the same forward with the configuration's 30-cell PML instead of Mur edges
+    pml = bench_pml(args, acq, waves, traces, device, barrier)
+
     # ---- FWI gradient, same grid and shots: forward with checkpoints + residual + adjoint
     grad = bench_gradient(args, acq, medium, rx, waves, traces, grad_tuning, device, world, barrier,
                           solver, sampler, tr)
@@ -508,6 +544,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_cores, "kind": "port", "sample": cpu_s},
             "grad": grad,
+            "pml": pml,
             "parity": parity,
             "gpu_launches": launches_per_pass * args.steps,
             "clocks": clocks.summary(),
