@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 4
+#define FDTD_ABI_VERSION 5
 
 enum {
   FDTD_OK = 0,
@@ -118,6 +118,18 @@ typedef struct fdtd_tuning {
 
 typedef struct fdtd_plan fdtd_plan; /* opaque host-side execution plan */
 
+/* Variable density (no reference counterpart in 2-D: the reference propagates
+   with constant density; its 1-D solver, 1DWaveSimulation.py:116-143, gives the
+   conservative form u_tt = rho c^2 div((1/rho) grad u) with 1/rho on the faces as
+   2 / (rho_a + rho_b)). fdtd_prepare_density fills the three device arrays; an
+   outer face takes its edge cell's rho. At constant rho the operator is the
+   reference's stencil. */
+typedef struct fdtd_density {
+  const float* kappa; /* device (ny, pitch): rho c^2 dt^2 */
+  const float* bx;    /* device (ny, pitch + 4): 1/rho on the face between columns x-1 and x, x = 0..nx */
+  const float* by;    /* device (ny + 1, pitch): 1/rho on the face between rows y-1 and y, y = 0..ny */
+} fdtd_density;
+
 /* ---------------------------------------------------------------- basics */
 int32_t fdtd_abi_version(void);
 const char* fdtd_last_error(void);
@@ -139,6 +151,12 @@ int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pit
 int32_t fdtd_prepare_medium_pml(const double* c, int32_t ny, int32_t nx, int32_t pitch,
                                 double dt, double dx, double dy, int32_t cells, double reflection,
                                 float* coef, float* mur, float* pml, void* stream);
+
+/* kappa, the face coefficients and the Mur table (from c, as fdtd_prepare_medium)
+   of a medium with sound speed c and density rho (device float64 (ny, nx)). */
+int32_t fdtd_prepare_density(const double* c, const double* rho, int32_t ny, int32_t nx, int32_t pitch,
+                             double dt, double dx, double dy, float* kappa, float* bx, float* by,
+                             float* mur, void* stream);
 
 /* ------------------------------------------------- one-step (plain) kernels */
 
@@ -173,6 +191,17 @@ int32_t fdtd_step_pml(const fdtd_grid* grid, int32_t n_shots,
                       const float* src_w, const int32_t* src_wave,
                       const float* waveforms, int32_t waveform_len, int32_t step,
                       const float* dense, int32_t adjoint, void* stream);
+
+/* fdtd_step with variable density: u_next = 2u - u_old + kappa D(b, u) + sources,
+   the reference's Mur edges (local sound speed); adjoint = 1 gives the reference's
+   adjoint form l_next = 2l - l_old + D(b, kappa l) + sources (adjoint = 2 is not
+   offered). No reference counterpart in 2-D. */
+int32_t fdtd_step_density(const fdtd_grid* grid, const fdtd_density* density, int32_t n_shots,
+                          const float* u_old, const float* u, float* u_next,
+                          int32_t src_per_shot, const int32_t* src_row, const int32_t* src_col,
+                          const float* src_w, const int32_t* src_wave,
+                          const float* waveforms, int32_t waveform_len, int32_t step,
+                          const float* dense, int32_t adjoint, void* stream);
 
 /* Bilinear receiver samples of a field batch:
    out[s * out_shot_stride + r * out_rx_stride] for s < n_shots, r < n_rx.
@@ -282,6 +311,29 @@ int32_t fdtd_gradient_plain(const fdtd_problem* problem, const float* observed,
                             const int32_t* mute, double* misfit, double* grad_c2,
                             void* workspace, size_t bytes, void* stream);
 size_t fdtd_gradient_plain_workspace(const fdtd_problem* problem);
+
+/* The plain per-shot forms with variable density (workspaces as fdtd_forward_plain
+   / fdtd_gradient_plain). The gradient adds dt^2 sum adj^n D(b, u^{n-1}) into
+   g_kappa (float64 (ny, pitch)) and, per face, dt^2 sum (adj_a kappa_a - adj_b
+   kappa_b) (u_b - u_a) / h^2 into g_bx (float64 (ny, pitch + 4)) and g_by (float64
+   (ny + 1, pitch)), kappa without dt^2 here: the derivatives of the misfit with
+   respect to rho c^2 and to the face coefficients 1/rho, the pairing of adjoint
+   and forward fields of the reference's imaging (invert_ring.py:683-701). No
+   reference counterpart in 2-D. */
+int32_t fdtd_forward_plain_density(const fdtd_problem* problem, const fdtd_density* density, float* traces,
+                                   void* workspace, size_t bytes, void* stream);
+int32_t fdtd_gradient_plain_density(const fdtd_problem* problem, const fdtd_density* density,
+                                    const float* observed, const int32_t* mute, double* misfit,
+                                    double* g_kappa, double* g_bx, double* g_by,
+                                    void* workspace, size_t bytes, void* stream);
+
+/* g_m = -g_kappa rho / m^2 and g_rho = g_kappa / m - sum over the cell's faces of
+   g_b b^2 / 2 (b^2 on an outer face), zero where mask == 0 (nullable): the chain
+   rule to slowness squared m = 1 / c^2 and density rho (float64, m and rho
+   (ny, nx), the gradients in the layouts above). */
+int32_t fdtd_density_chain_rule(int32_t ny, int32_t nx, int32_t pitch, const double* m, const double* rho,
+                                const double* g_kappa, const double* g_bx, const double* g_by,
+                                const uint8_t* mask, double* g_m, double* g_rho, void* stream);
 
 /* Size of the fixed device scratch behind fdtd_forward_plain_static: three
    fields of one shot plus the receiver and source tables must fit (about

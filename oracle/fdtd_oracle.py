@@ -642,3 +642,125 @@ def analytic_line_source(r, t, h, dt_sim, pulse, c=1500.0, dt_a=None):
     u = np.fft.irfft(np.fft.rfft(s, m) * np.fft.rfft(G, m), m)[:n] / (2 * np.pi * c ** 2)
     u *= h ** 2 / dt_sim ** 2
     return np.interp(t, ta + dt_a, u)
+
+
+# ---------------------------------------------------------------------------
+# Variable density (no reference counterpart in 2-D: the reference propagates
+# with constant density, FWI_Technical_Note.tex:56-59, and only plans the
+# conservative form at fdtd2d/wave.py:61-63). The 1-D solver of
+# 1DWaveSimulation.py:116-143 gives the discretisation: u_tt = rho c^2
+# d/dx((1/rho) du/dx) with 1/rho on the faces as 2 / (rho_a + rho_b). Own float64
+# restatement in 2-D; at constant rho it is the reference's stencil.
+# ---------------------------------------------------------------------------
+
+def density_faces(rho):
+    """Face coefficients b = 1/rho: bx (ny, nx + 1) on the faces between columns
+    x-1 and x (x = 0..nx; the outer faces take the edge cell's own rho) and by
+    (ny + 1, nx) between rows."""
+    r = np.asarray(rho, dtype=float)
+    rx = np.concatenate([r[:, :1], r, r[:, -1:]], axis=1)
+    ry = np.concatenate([r[:1, :], r, r[-1:, :]], axis=0)
+    return 2.0 / (rx[:, 1:] + rx[:, :-1]), 2.0 / (ry[1:, :] + ry[:-1, :])
+
+
+def density_operator(u, bx, by, dx, dy):
+    """D(b, u) = d/dx(b du/dx) + d/dy(b du/dy) on faces, zero beyond the grid."""
+    zx = np.zeros(u.shape[:-1] + (1,))
+    zy = np.zeros(u.shape[:-2] + (1, u.shape[-1]))
+    fx = bx * np.diff(np.concatenate([zx, u, zx], axis=-1), axis=-1) / (dx * dx)   # (.., ny, nx + 1)
+    fy = by * np.diff(np.concatenate([zy, u, zy], axis=-2), axis=-2) / (dy * dy)   # (.., ny + 1, nx)
+    return np.diff(fx, axis=-1) + np.diff(fy, axis=-2)
+
+
+def simulate_density(c, rho, dx, dy, dt, geo, source_fields, source_values, n_steps, store=False):
+    """Batched forward u+ = 2u - u- + dt^2 rho c^2 D(1/rho, u) + s with the
+    reference's Mur edges (the local sound speed, fdtd2d/solver.py:90-124):
+    traces (S, R, n_steps), and with ``store`` every field (n_steps, S, ny, nx)."""
+    c = np.asarray(c, dtype=float)
+    rho = np.asarray(rho, dtype=float)
+    kap = dt * dt * rho * c * c
+    bx, by = density_faces(rho)
+    k = mur_coefficients(c, dt, dx, dy)
+    fields = np.asarray(source_fields, dtype=float)
+    S = fields.shape[0]
+    values = np.asarray(source_values, dtype=float)
+    if values.ndim == 1:
+        values = np.broadcast_to(values, (S, values.shape[0]))
+    u_old = np.zeros((S,) + c.shape)
+    u = np.zeros_like(u_old)
+    traces = np.zeros((S, len(geo["row0"]), n_steps))
+    wave = np.zeros((n_steps,) + u.shape) if store else None
+    for step in range(n_steps):
+        u_next = 2.0 * u - u_old + kap * density_operator(u, bx, by, dx, dy)
+        if step < values.shape[1]:
+            u_next = u_next + fields * values[:, step, None, None]
+        u_next = apply_mur(u, u_next, k)
+        u_old, u = u, u_next
+        traces[:, :, step] = gather(u, geo)
+        if store:
+            wave[step] = u
+    return traces, wave
+
+
+def density_gradient(c, rho, dx, dy, dt, geo, source_fields, source_values, n_steps, observed, mute):
+    """Misfit and the gradients with respect to kappa = rho c^2 (per cell) and to
+    the face coefficients bx, by, by the reverse-time loop of
+    adjoint_gradient_c2 with the density operator: l+ = 2l - l- + D(b, dt^2 kappa l)
+    + scatter(residual), the forward Mur, and for n >= 1
+      g_kappa += dt^2 l+ D(b, u^{n-1}),
+      g_bx(face x-1|x) += dt^2 (dt^2... per face: (l+_{x-1} kappa_{x-1} - l+_x kappa_x)
+                          (u_x - u_{x-1}) / dx^2, and the same for by,
+    the same pairing of adjoint and forward fields as the reference's imaging
+    (invert_ring.py:683-701). Returns (misfit, g_kappa, g_bx, g_by)."""
+    c = np.asarray(c, dtype=float)
+    rho = np.asarray(rho, dtype=float)
+    kap = rho * c * c
+    bx, by = density_faces(rho)
+    k = mur_coefficients(c, dt, dx, dy)
+    traces, wave = simulate_density(c, rho, dx, dy, dt, geo, source_fields, source_values, n_steps, store=True)
+    residual = residual_batch(traces, np.asarray(observed, dtype=float), mute)
+    misfit = 0.5 * float(np.sum(residual ** 2))
+    S = residual.shape[0]
+    l_old = np.zeros((S,) + c.shape)
+    lam = np.zeros_like(l_old)
+    gk = np.zeros(c.shape)
+    gbx = np.zeros(bx.shape)
+    gby = np.zeros(by.shape)
+    dt2 = dt * dt
+    zx = np.zeros((S, c.shape[0], 1))
+    zy = np.zeros((S, 1, c.shape[1]))
+    for n in range(n_steps - 1, -1, -1):
+        src = scatter(residual[:, :, n], geo, c.shape)
+        l_next = 2.0 * lam - l_old + density_operator(dt2 * kap * lam, bx, by, dx, dy) + src
+        l_next = apply_mur(lam, l_next, k)
+        l_old, lam = lam, l_next
+        if n > 0:
+            u = wave[n - 1]
+            gk += dt2 * np.sum(lam * density_operator(u, bx, by, dx, dy), axis=0)
+            w = lam * kap
+            wx = np.concatenate([zx, w, zx], axis=-1)
+            ux = np.concatenate([zx, u, zx], axis=-1)
+            gbx += dt2 * np.sum(-np.diff(wx, axis=-1) * np.diff(ux, axis=-1), axis=0) / (dx * dx)
+            wy = np.concatenate([zy, w, zy], axis=-2)
+            uy = np.concatenate([zy, u, zy], axis=-2)
+            gby += dt2 * np.sum(-np.diff(wy, axis=-2) * np.diff(uy, axis=-2), axis=0) / (dy * dy)
+    return misfit, gk, gbx, gby
+
+
+def density_chain_rule(m, rho, g_kappa, g_bx, g_by):
+    """g_m and g_rho from the kappa and face gradients, with kappa = rho / m and
+    b = 2 / (rho_a + rho_b) (an outer face: 1 / rho of its edge cell)."""
+    m = np.asarray(m, dtype=float)
+    rho = np.asarray(rho, dtype=float)
+    bx, by = density_faces(rho)
+    g_m = -g_kappa * rho / (m * m)
+    g_rho = g_kappa / m
+    # interior faces: db/drho_a = -b^2 / 2 for both cells; outer faces: -b^2
+    hx = -0.5 * g_bx * bx * bx
+    hy = -0.5 * g_by * by * by
+    g_rho = g_rho + hx[:, :-1] + hx[:, 1:] + hy[:-1, :] + hy[1:, :]
+    g_rho[:, 0] += hx[:, 0]
+    g_rho[:, -1] += hx[:, -1]
+    g_rho[0, :] += hy[0, :]
+    g_rho[-1, :] += hy[-1, :]
+    return g_m, g_rho

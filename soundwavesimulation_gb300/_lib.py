@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "libfdtd_gb300.so"
-ABI_VERSION = 4
+ABI_VERSION = 5
 
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 
@@ -23,6 +23,10 @@ class Grid(ctypes.Structure):
     _fields_ = [("ny", c_int32), ("nx", c_int32), ("pitch", c_int32),
                 ("dx", c_double), ("dy", c_double), ("dt", c_double),
                 ("coef", c_void_p), ("mur", c_void_p), ("pml", c_void_p), ("pml_cells", c_int32)]
+
+
+class Density(ctypes.Structure):
+    _fields_ = [("kappa", c_void_p), ("bx", c_void_p), ("by", c_void_p)]
 
 
 class Receivers(ctypes.Structure):
@@ -102,6 +106,17 @@ _SIGNATURES = {
     "fdtd_forward_plain_static": (c_int32, [POINTER(Problem), c_void_p, c_void_p]),
     "fdtd_tile_axis": (c_int32, [c_int32, c_int32, c_int32, c_int32, c_int32, c_int32,
                                  c_void_p, POINTER(c_int32)]),
+    "fdtd_prepare_density": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_double, c_double, c_double,
+                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fdtd_step_density": (c_int32, [POINTER(Grid), POINTER(Density), c_int32, c_void_p, c_void_p, c_void_p, c_int32,
+                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
+                                    c_void_p, c_int32, c_void_p]),
+    "fdtd_forward_plain_density": (c_int32, [POINTER(Problem), POINTER(Density), c_void_p, c_void_p, c_size_t,
+                                             c_void_p]),
+    "fdtd_gradient_plain_density": (c_int32, [POINTER(Problem), POINTER(Density), c_void_p, c_void_p, c_void_p,
+                                              c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "fdtd_density_chain_rule": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
+                                          c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fdtd_autotune_workspace_bytes": (c_size_t, [POINTER(Problem), c_int32, c_int32]),
     "fdtd_autotune": (c_int32, [POINTER(Problem), c_int32, c_int32, c_int32, c_void_p, c_size_t,
                                 POINTER(Tuning), POINTER(c_double), c_void_p, c_void_p, POINTER(c_int32),
@@ -166,5 +181,5 @@ def tap_table(ny, nx, row0, col0, weights):
     return nodes[:n.value].copy(), tw[:n.value].copy()
 
 
-__all__ = ["Grid", "Receivers", "Sources", "Problem", "Tuning", "load", "check", "tile_axis",
+__all__ = ["Grid", "Density", "Receivers", "Sources", "Problem", "Tuning", "load", "check", "tile_axis",
            "tap_table", "EXPORTED", "STORE_F32", "STORE_F16", "STORE_BF16", "c_float"]

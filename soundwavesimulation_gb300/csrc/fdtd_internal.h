@@ -54,8 +54,26 @@ struct StepArgs {
   int step;
   const float* dense;
   int adjoint;
+  // variable density (kap != nullptr): rho c^2 dt^2 per cell and 1/rho on the
+  // faces, bx (ny, pitch + 4) between columns x-1 and x, by (ny + 1, pitch)
+  const float* kap = nullptr;
+  const float* bx = nullptr;
+  const float* by = nullptr;
 };
 cudaError_t step_launch(const StepArgs& a, cudaStream_t st);
+// Variable density: kappa = rho c^2 dt^2, the face coefficients and the Mur table.
+cudaError_t prepare_density_launch(const double* c, const double* rho, int ny, int nx, int pitch, double dt,
+                                   double dx, double dy, float* kap, float* bx, float* by, float* mur,
+                                   cudaStream_t st);
+// Imaging of a variable-density step: g_kappa += scale sum_s adj D(b, fwd) per cell,
+// and per face g_b += scale sum_s (adj_a kappa_a - adj_b kappa_b) (fwd_b - fwd_a) / h^2
+// (kappa without dt^2: kap / dt2).
+cudaError_t image_density_launch(int ny, int nx, int pitch, float idx2, float idy2, int n_shots, const float* adj,
+                                 const float* fwd, const float* kap, const float* bx, const float* by, double scale,
+                                 double dt2, double* gk, double* gbx, double* gby, cudaStream_t st);
+cudaError_t density_chain_launch(int ny, int nx, int pitch, const double* m, const double* rho,
+                                 const double* gk, const double* gbx, const double* gby, const uint8_t* mask,
+                                 double* g_m, double* g_rho, cudaStream_t st);
 // One step of a PML grid (fdtd_step_pml): tables, dt / 2, dt^2 and the face fields.
 cudaError_t step_pml_launch(const StepArgs& a, const float* pml, float hdt, float dt2, const float* psx,
                             const float* psy, float* psx_next, float* psy_next, cudaStream_t st);

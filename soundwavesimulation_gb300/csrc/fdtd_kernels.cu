@@ -17,12 +17,50 @@ __device__ __forceinline__ float operand(const StepArgs& a, const float* u, int 
   return a.adjoint == 1 ? __fmul_rn(a.coef[i], v) : v;
 }
 
+// D(b, u) = ((b_r (u_r - u) - b_l (u - u_l)) / dx^2 + (b_t (u_t - u) - b_b (u - u_b)) / dy^2:
+// the conservative operator of 1DWaveSimulation.py:116-143 in 2-D.
+__device__ __forceinline__ float dens_op(float c, float l, float r, float d, float t, float bl, float br, float bb,
+                                         float bt, float idx2, float idy2) {
+  const float fx = __fsub_rn(__fmul_rn(br, __fsub_rn(r, c)), __fmul_rn(bl, __fsub_rn(c, l)));
+  const float fy = __fsub_rn(__fmul_rn(bt, __fsub_rn(t, c)), __fmul_rn(bb, __fsub_rn(c, d)));
+  return __fmaf_rn(fy, idy2, __fmul_rn(fx, idx2));
+}
+
+__device__ __forceinline__ float dens_operand(const StepArgs& a, const float* u, int y, int x) {
+  if (y < 0 || y >= a.ny || x < 0 || x >= a.nx) return 0.f;
+  const long long i = (long long)y * a.pitch + x;
+  return a.adjoint == 1 ? __fmul_rn(a.kap[i], u[i]) : u[i];
+}
+
 // Interior update of node (y, x) of shot s, sources included, before Mur.
 __device__ float cell_next(const StepArgs& a, int s, int y, int x) {
   const long long plane = (long long)a.ny * a.pitch;
   const float* u = a.u + s * plane;
   const float* uo = a.u_old + s * plane;
   const long long i = (long long)y * a.pitch + x;
+  if (a.kap) {
+    // variable density: u+ = 2u - u- + kap D(b, u); the adjoint (1): l+ = 2l - l- + D(b, kap l)
+    const long long bxs = a.pitch + 4;
+    const float D = dens_op(dens_operand(a, u, y, x), dens_operand(a, u, y, x - 1), dens_operand(a, u, y, x + 1),
+                            dens_operand(a, u, y - 1, x), dens_operand(a, u, y + 1, x), a.bx[y * bxs + x],
+                            a.bx[y * bxs + x + 1], a.by[i], a.by[i + a.pitch], a.idx2, a.idy2);
+    float un = a.adjoint == 1 ? leap_adj(u[i], uo[i], D) : leap(u[i], uo[i], a.kap[i], D);
+    if (a.src_per_shot > 0) {
+      float acc = 0.f;
+      bool hit = false;
+      for (int j = 0; j < a.src_per_shot; ++j) {
+        const int e = s * a.src_per_shot + j;
+        if (a.src_row[e] == y && a.src_col[e] == x && a.src_wave[e] >= 0) {
+          const float v = (a.step < a.wave_len) ? a.waveforms[(long long)a.src_wave[e] * a.wave_len + a.step] : 0.f;
+          acc = inj_acc(acc, a.src_w[e], v);
+          hit = true;
+        }
+      }
+      if (hit) un = inj_add(un, acc);
+    }
+    if (a.dense) un = inj_add(un, a.dense[s * plane + i]);
+    return un;
+  }
   const float nb = nbr4(operand(a, u, y, x - 1), operand(a, u, y, x + 1), operand(a, u, y - 1, x),
                         operand(a, u, y + 1, x), a.idx2, a.idy2);
   const float lap = __fmaf_rn(operand(a, u, y, x), a.cdiag, nb);
@@ -207,6 +245,100 @@ __global__ void pml_prepare_kernel(const double* c, int ny, int nx, int pitch, d
     const double cd = c[k] * dt;
     coef[(long long)y * pitch + x] = (float)(cd * cd * q);
   }
+}
+
+// kappa = rho c^2 dt^2 (ny, pitch) and the face coefficients 1/rho = 2 / (rho_a +
+// rho_b), an outer face taking its edge cell's rho: bx (ny, pitch + 4), by (ny + 1, pitch).
+__global__ void density_prepare_kernel(const double* c, const double* rho, int ny, int nx, int pitch, double dt,
+                                       float* kap, float* bx, float* by) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (y < ny && x < pitch) {
+    float v = 0.f;
+    if (x < nx) {
+      const double cc = c[(long long)y * nx + x];
+      v = (float)(dt * dt * rho[(long long)y * nx + x] * cc * cc);
+    }
+    kap[(long long)y * pitch + x] = v;
+  }
+  if (y < ny && x < pitch + 4) {
+    float v = 0.f;
+    if (x <= nx) {
+      const int xa = x > 0 ? x - 1 : 0, xb = x < nx ? x : nx - 1;
+      v = (float)(2.0 / (rho[(long long)y * nx + xa] + rho[(long long)y * nx + xb]));
+    }
+    bx[(long long)y * (pitch + 4) + x] = v;
+  }
+  if (y <= ny && x < pitch) {
+    float v = 0.f;
+    if (x < nx) {
+      const int ya = y > 0 ? y - 1 : 0, yb = y < ny ? y : ny - 1;
+      v = (float)(2.0 / (rho[(long long)ya * nx + x] + rho[(long long)yb * nx + x]));
+    }
+    by[(long long)y * pitch + x] = v;
+  }
+}
+
+// One variable-density step's imaging (see image_density_launch): thread (y, x)
+// owns cell (y, x), the x-face to its left (x = 0..nx) and the y-face below it
+// (y = 0..ny), and sums the shots itself (no atomics).
+__global__ void image_density_kernel(int ny, int nx, int pitch, float idx2, float idy2, int n_shots,
+                                     const float* __restrict__ adj, const float* __restrict__ fwd,
+                                     const float* __restrict__ kap, const float* __restrict__ bx,
+                                     const float* __restrict__ by, double scale, double dt2, double* gk,
+                                     double* gbx, double* gby) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const long long plane = (long long)ny * pitch, bxs = pitch + 4;
+  auto F = [&](const float* f, int yy, int xx) {
+    return (yy < 0 || yy >= ny || xx < 0 || xx >= nx) ? 0.f : f[(long long)yy * pitch + xx];
+  };
+  auto K = [&](int yy, int xx) {  // kappa without dt^2, float64
+    return (yy < 0 || yy >= ny || xx < 0 || xx >= nx) ? 0.0 : (double)kap[(long long)yy * pitch + xx] / dt2;
+  };
+  double sk = 0.0, sx = 0.0, sy = 0.0;
+  for (int s = 0; s < n_shots; ++s) {
+    const float* w = adj + s * plane;
+    const float* u = fwd + s * plane;
+    if (y < ny && x < nx) {
+      const long long i = (long long)y * pitch + x;
+      const float D = dens_op(u[i], F(u, y, x - 1), F(u, y, x + 1), F(u, y - 1, x), F(u, y + 1, x), bx[y * bxs + x],
+                              bx[y * bxs + x + 1], by[i], by[i + pitch], idx2, idy2);
+      sk += (double)w[i] * (double)D;
+    }
+    if (y < ny && x <= nx)
+      sx += (K(y, x - 1) * F(w, y, x - 1) - K(y, x) * F(w, y, x)) * ((double)F(u, y, x) - F(u, y, x - 1));
+    if (y <= ny && x < nx)
+      sy += (K(y - 1, x) * F(w, y - 1, x) - K(y, x) * F(w, y, x)) * ((double)F(u, y, x) - F(u, y - 1, x));
+  }
+  if (y < ny && x < nx) gk[(long long)y * pitch + x] += scale * sk;
+  if (y < ny && x <= nx) gbx[(long long)y * bxs + x] += scale * sx * (double)idx2;
+  if (y <= ny && x < nx) gby[(long long)y * pitch + x] += scale * sy * (double)idy2;
+}
+
+// g_m = -g_kappa rho / m^2 and g_rho = g_kappa / m + the face terms (db/drho = -b^2 / 2
+// on an interior face, -b^2 on an outer one), zero off the mask.
+__global__ void density_chain_kernel(int ny, int nx, int pitch, const double* m, const double* rho,
+                                     const double* gk, const double* gbx, const double* gby, const uint8_t* mask,
+                                     double* g_m, double* g_rho) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= nx || y >= ny) return;
+  const long long i = (long long)y * nx + x, bxs = pitch + 4;
+  auto R = [&](int yy, int xx) { return rho[(long long)yy * nx + xx]; };
+  auto face = [](double ra, double rb) { const double b = 2.0 / (ra + rb); return b * b; };
+  const double mi = m[i], ri = R(y, x);
+  const double g = gk[(long long)y * pitch + x];
+  double gr = g / mi;
+  const double hl = -0.5 * gbx[y * bxs + x] * face(x > 0 ? R(y, x - 1) : ri, ri);
+  const double hr = -0.5 * gbx[y * bxs + x + 1] * face(ri, x + 1 < nx ? R(y, x + 1) : ri);
+  const double hb = -0.5 * gby[(long long)y * pitch + x] * face(y > 0 ? R(y - 1, x) : ri, ri);
+  const double ht = -0.5 * gby[(long long)(y + 1) * pitch + x] * face(ri, y + 1 < ny ? R(y + 1, x) : ri);
+  gr += (x == 0 ? 2.0 : 1.0) * hl + (x == nx - 1 ? 2.0 : 1.0) * hr + (y == 0 ? 2.0 : 1.0) * hb +
+        (y == ny - 1 ? 2.0 : 1.0) * ht;
+  const bool in = !mask || mask[i];
+  g_m[i] = in ? -g * ri / (mi * mi) : 0.0;
+  g_rho[i] = in ? gr : 0.0;
 }
 
 __global__ void gather_kernel(int pitch, long long plane, int n_shots, const float* f, int n_rx,
@@ -477,6 +609,38 @@ cudaError_t step_pml_launch(const StepArgs& a, const float* pml, float hdt, floa
 cudaError_t prepare_pml_launch(const double* c, int ny, int nx, int pitch, double dt, double dx, double dy,
                                int cells, double reflection, float* coef, float* pml, cudaStream_t st) {
   pml_prepare_kernel<<<1, 1024, 0, st>>>(c, ny, nx, pitch, dt, dx, dy, cells, reflection, coef, pml);
+  return cudaGetLastError();
+}
+
+cudaError_t prepare_density_launch(const double* c, const double* rho, int ny, int nx, int pitch, double dt,
+                                   double dx, double dy, float* kap, float* bx, float* by, float* mur,
+                                   cudaStream_t st) {
+  dim3 block(32, 8);
+  dim3 grid((pitch + 4 + 31) / 32, (ny + 1 + 7) / 8);
+  density_prepare_kernel<<<grid, block, 0, st>>>(c, rho, ny, nx, pitch, dt, kap, bx, by);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int n = (ny > nx ? ny : nx);
+  mur_kernel<<<(n + 255) / 256, 256, 0, st>>>(c, ny, nx, dt, dx, dy, mur);
+  return cudaGetLastError();
+}
+
+cudaError_t image_density_launch(int ny, int nx, int pitch, float idx2, float idy2, int n_shots, const float* adj,
+                                 const float* fwd, const float* kap, const float* bx, const float* by, double scale,
+                                 double dt2, double* gk, double* gbx, double* gby, cudaStream_t st) {
+  dim3 block(32, 8);
+  dim3 grid((nx + 1 + 31) / 32, (ny + 1 + 7) / 8);
+  image_density_kernel<<<grid, block, 0, st>>>(ny, nx, pitch, idx2, idy2, n_shots, adj, fwd, kap, bx, by, scale,
+                                               dt2, gk, gbx, gby);
+  return cudaGetLastError();
+}
+
+cudaError_t density_chain_launch(int ny, int nx, int pitch, const double* m, const double* rho,
+                                 const double* gk, const double* gbx, const double* gby, const uint8_t* mask,
+                                 double* g_m, double* g_rho, cudaStream_t st) {
+  dim3 block(32, 8);
+  dim3 grid((nx + 31) / 32, (ny + 7) / 8);
+  density_chain_kernel<<<grid, block, 0, st>>>(ny, nx, pitch, m, rho, gk, gbx, gby, mask, g_m, g_rho);
   return cudaGetLastError();
 }
 

@@ -613,8 +613,14 @@ int32_t fdtd_step_pml(const fdtd_grid* grid, int32_t n_shots, const float* u_old
   return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "fdtd_step_pml");
 }
 
-int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, const float* u,
-                  float* u_next, int32_t src_per_shot, const int32_t* src_row,
+}  // extern "C"
+
+namespace {
+
+// One step of the one-step kernel for the Mur grid, or with `density` the
+// variable-density operator (adjoint 0 or 1).
+int32_t step_impl(const fdtd_grid* grid, const fdtd_density* density, int32_t n_shots, const float* u_old,
+                  const float* u, float* u_next, int32_t src_per_shot, const int32_t* src_row,
                   const int32_t* src_col, const float* src_w, const int32_t* src_wave,
                   const float* waveforms, int32_t waveform_len, int32_t step, const float* dense,
                   int32_t adjoint, void* stream) {
@@ -652,9 +658,58 @@ int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, co
   a.dense = dense;
   if (adjoint < 0 || adjoint > 2) return fail(FDTD_ERR_INVALID, "adjoint must be 0, 1 or 2");
   a.adjoint = adjoint;
+  if (density) {
+    if (!density->kappa || !density->bx || !density->by) return fail(FDTD_ERR_INVALID, "density arrays missing");
+    if (adjoint == 2) return fail(FDTD_ERR_INVALID, "a variable-density step takes adjoint 0 or 1");
+    a.kap = density->kappa;
+    a.bx = density->bx;
+    a.by = density->by;
+  }
   cudaError_t e = step_launch(a, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "step");
   return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fdtd_step(const fdtd_grid* grid, int32_t n_shots, const float* u_old, const float* u,
+                  float* u_next, int32_t src_per_shot, const int32_t* src_row,
+                  const int32_t* src_col, const float* src_w, const int32_t* src_wave,
+                  const float* waveforms, int32_t waveform_len, int32_t step, const float* dense,
+                  int32_t adjoint, void* stream) {
+  return step_impl(grid, nullptr, n_shots, u_old, u, u_next, src_per_shot, src_row, src_col, src_w, src_wave,
+                   waveforms, waveform_len, step, dense, adjoint, stream);
+}
+
+int32_t fdtd_step_density(const fdtd_grid* grid, const fdtd_density* density, int32_t n_shots, const float* u_old,
+                          const float* u, float* u_next, int32_t src_per_shot, const int32_t* src_row,
+                          const int32_t* src_col, const float* src_w, const int32_t* src_wave,
+                          const float* waveforms, int32_t waveform_len, int32_t step, const float* dense,
+                          int32_t adjoint, void* stream) {
+  if (!density) return fail(FDTD_ERR_INVALID, "null density");
+  return step_impl(grid, density, n_shots, u_old, u, u_next, src_per_shot, src_row, src_col, src_w, src_wave,
+                   waveforms, waveform_len, step, dense, adjoint, stream);
+}
+
+int32_t fdtd_prepare_density(const double* c, const double* rho, int32_t ny, int32_t nx, int32_t pitch, double dt,
+                             double dx, double dy, float* kappa, float* bx, float* by, float* mur, void* stream) {
+  if (!c || !rho || !kappa || !bx || !by || !mur) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (ny < 3 || nx < 3 || pitch < nx || pitch % 4) return fail(FDTD_ERR_INVALID, "bad grid shape");
+  if (!(dt > 0) || !(dx > 0) || !(dy > 0)) return fail(FDTD_ERR_INVALID, "dx, dy and dt must be positive");
+  cudaError_t e = prepare_density_launch(c, rho, ny, nx, pitch, dt, dx, dy, kappa, bx, by, mur, (cudaStream_t)stream);
+  return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "prepare_density");
+}
+
+int32_t fdtd_density_chain_rule(int32_t ny, int32_t nx, int32_t pitch, const double* m, const double* rho,
+                                const double* g_kappa, const double* g_bx, const double* g_by, const uint8_t* mask,
+                                double* g_m, double* g_rho, void* stream) {
+  if (!m || !rho || !g_kappa || !g_bx || !g_by || !g_m || !g_rho) return fail(FDTD_ERR_INVALID, "null pointer");
+  if (ny < 3 || nx < 3 || pitch < nx) return fail(FDTD_ERR_INVALID, "bad grid shape");
+  cudaError_t e = density_chain_launch(ny, nx, pitch, m, rho, g_kappa, g_bx, g_by, mask, g_m, g_rho,
+                                       (cudaStream_t)stream);
+  return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "density_chain_rule");
 }
 
 int32_t fdtd_gather(const fdtd_grid* grid, int32_t n_shots, const float* fields, int32_t n_rx,
@@ -1437,8 +1492,12 @@ size_t fdtd_forward_plain_workspace(const fdtd_problem* prob) {
          align_up((size_t)prob->n_shots * K * (3 * sizeof(int32_t) + sizeof(float)) + 16);
 }
 
-int32_t fdtd_forward_plain(const fdtd_problem* prob, float* traces, void* workspace, size_t bytes,
-                           void* stream) {
+}  // extern "C"
+
+namespace {
+
+int32_t forward_plain_impl(const fdtd_problem* prob, const fdtd_density* density, float* traces, void* workspace,
+                           size_t bytes, void* stream) {
   if (!prob || !traces) return fail(FDTD_ERR_INVALID, "null argument");
   int32_t rc = validate_plain_problem(*prob);
   if (rc) return rc;
@@ -1477,7 +1536,7 @@ int32_t fdtd_forward_plain(const fdtd_problem* prob, float* traces, void* worksp
     if (e != cudaSuccess) return cuda_fail(e, "plain forward reset");
     int io = 0, ic = 1, in = 2;
     for (int n = 0; n < nt; ++n) {
-      rc = fdtd_step(&g, 1, f[io], f[ic], f[in], K, s_row + (size_t)s * K, s_col + (size_t)s * K,
+      rc = step_impl(&g, density, 1, f[io], f[ic], f[in], K, s_row + (size_t)s * K, s_col + (size_t)s * K,
                      s_w + (size_t)s * K, s_wave + (size_t)s * K, prob->src.waveforms,
                      prob->src.waveform_len, n, nullptr, 0, stream);
       if (rc) return rc;
@@ -1489,6 +1548,21 @@ int32_t fdtd_forward_plain(const fdtd_problem* prob, float* traces, void* worksp
   return FDTD_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int32_t fdtd_forward_plain(const fdtd_problem* prob, float* traces, void* workspace, size_t bytes,
+                           void* stream) {
+  return forward_plain_impl(prob, nullptr, traces, workspace, bytes, stream);
+}
+
+int32_t fdtd_forward_plain_density(const fdtd_problem* prob, const fdtd_density* density, float* traces,
+                                   void* workspace, size_t bytes, void* stream) {
+  if (!density) return fail(FDTD_ERR_INVALID, "null density");
+  return forward_plain_impl(prob, density, traces, workspace, bytes, stream);
+}
+
 size_t fdtd_gradient_plain_workspace(const fdtd_problem* prob) {
   if (!prob) return 0;
   const size_t plane = (size_t)prob->grid.ny * prob->grid.pitch * sizeof(float);
@@ -1497,10 +1571,18 @@ size_t fdtd_gradient_plain_workspace(const fdtd_problem* prob) {
          align_up(2 * R * nt * sizeof(float)) + align_up(4 * R * (10 + 8) * sizeof(int32_t));
 }
 
-int32_t fdtd_gradient_plain(const fdtd_problem* prob, const float* observed, const int32_t* mute,
-                            double* misfit, double* grad_c2, void* workspace, size_t bytes,
-                            void* stream) {
+}  // extern "C"
+
+namespace {
+
+// The plain per-shot gradient; with `density` the variable-density operator, the
+// adjoint in the reference's l form and the imaging into g_kappa (grad_c2) and the
+// face gradients g_bx (ny, pitch + 4), g_by (ny + 1, pitch).
+int32_t gradient_plain_impl(const fdtd_problem* prob, const fdtd_density* density, const float* observed,
+                            const int32_t* mute, double* misfit, double* grad_c2, double* g_bx, double* g_by,
+                            void* workspace, size_t bytes, void* stream) {
   if (!prob || !observed || !misfit || !grad_c2) return fail(FDTD_ERR_INVALID, "null argument");
+  if (density && (!g_bx || !g_by)) return fail(FDTD_ERR_INVALID, "face gradients missing");
   int32_t rc = validate_plain_problem(*prob);
   if (rc) return rc;
   if (!workspace || bytes < fdtd_gradient_plain_workspace(prob)) return fail(FDTD_ERR_WORKSPACE, "workspace too small");
@@ -1557,7 +1639,7 @@ int32_t fdtd_gradient_plain(const fdtd_problem* prob, const float* observed, con
     if (e != cudaSuccess) return cuda_fail(e, "plain gradient reset");
     for (int n = 0; n < nt; ++n) {
       float* un = hist + (size_t)(n + 2) * plane;
-      rc = fdtd_step(&g, 1, hist + (size_t)n * plane, hist + (size_t)(n + 1) * plane, un, K,
+      rc = step_impl(&g, density, 1, hist + (size_t)n * plane, hist + (size_t)(n + 1) * plane, un, K,
                      s_row + (size_t)s * K, s_col + (size_t)s * K, s_w + (size_t)s * K,
                      s_wave + (size_t)s * K, prob->src.waveforms, prob->src.waveform_len, n,
                      nullptr, 0, stream);
@@ -1575,11 +1657,17 @@ int32_t fdtd_gradient_plain(const fdtd_problem* prob, const float* observed, con
     for (int n = nt - 1; n >= 0; --n) {
       e = scatter_launch(g.ny, g.pitch, 1, n_nodes, tap_nodes, tap_w, resid + n, 0, nt, dense, st);
       if (e != cudaSuccess) return cuda_fail(e, "plain scatter");
-      // the adjoint in w = coef * l form, as the fused engine carries it
-      rc = fdtd_step(&g, 1, lam + (size_t)io * plane, lam + (size_t)ic * plane, lam + (size_t)in * plane, 0,
-                     nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, dense, 2, stream);
+      // the adjoint in w = coef * l form, as the fused engine carries it; with
+      // variable density in the reference's l form
+      rc = step_impl(&g, density, 1, lam + (size_t)io * plane, lam + (size_t)ic * plane, lam + (size_t)in * plane,
+                     0, nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, dense, density ? 1 : 2, stream);
       if (rc) return rc;
-      if (n >= 1) {
+      if (n >= 1 && density) {
+        e = image_density_launch(g.ny, g.nx, g.pitch, (float)idx2, (float)idy2, 1, lam + (size_t)in * plane,
+                                 hist + (size_t)(n + 1) * plane, density->kappa, density->bx, density->by,
+                                 g.dt * g.dt, g.dt * g.dt, grad_c2, g_bx, g_by, st);
+        if (e != cudaSuccess) return cuda_fail(e, "plain density image");
+      } else if (n >= 1) {
         e = image_launch(g.ny, g.nx, g.pitch, (float)idx2, (float)idy2, (float)(-2.0 * (idx2 + idy2)), 1,
                          lam + (size_t)in * plane, hist + (size_t)(n + 1) * plane, g.dt * g.dt, g.coef,
                          grad_c2, st);
@@ -1589,6 +1677,24 @@ int32_t fdtd_gradient_plain(const fdtd_problem* prob, const float* observed, con
     }
   }
   return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fdtd_gradient_plain(const fdtd_problem* prob, const float* observed, const int32_t* mute,
+                            double* misfit, double* grad_c2, void* workspace, size_t bytes,
+                            void* stream) {
+  return gradient_plain_impl(prob, nullptr, observed, mute, misfit, grad_c2, nullptr, nullptr, workspace, bytes,
+                             stream);
+}
+
+int32_t fdtd_gradient_plain_density(const fdtd_problem* prob, const fdtd_density* density, const float* observed,
+                                    const int32_t* mute, double* misfit, double* g_kappa, double* g_bx,
+                                    double* g_by, void* workspace, size_t bytes, void* stream) {
+  if (!density) return fail(FDTD_ERR_INVALID, "null density");
+  return gradient_plain_impl(prob, density, observed, mute, misfit, g_kappa, g_bx, g_by, workspace, bytes, stream);
 }
 
 }  // extern "C"
