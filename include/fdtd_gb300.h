@@ -114,7 +114,18 @@ typedef struct fdtd_tuning {
   int32_t eager;            /* 0 (default): fdtd_forward / fdtd_adjoint capture their launch
                                sequence once per set of output pointers and replay it as a
                                CUDA graph; 1: launch every kernel from the host */
+  int32_t step_sync;        /* FDTD_SYNC_*: how the warps of a CTA meet after every step */
 } fdtd_tuning;
+
+/* Step synchronisation of the temporally blocked kernel. After every leapfrog step
+   a warp has published the first and last row of its band, which only the warps
+   above and below read: FDTD_SYNC_PAIR meets each neighbouring pair of warps on
+   its own hardware barrier, so warps further apart drift by up to their distance
+   in steps; FDTD_SYNC_CTA meets the whole CTA. FDTD_SYNC_AUTO takes PAIR up to
+   16 warps (15 named barriers) and CTA beyond. */
+#define FDTD_SYNC_AUTO 0
+#define FDTD_SYNC_CTA 1
+#define FDTD_SYNC_PAIR 2
 
 typedef struct fdtd_plan fdtd_plan; /* opaque host-side execution plan */
 

@@ -47,7 +47,7 @@ class Problem(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("rows_per_lane", c_int32), ("warps", c_int32), ("steps_per_launch", c_int32),
                 ("ckpt_every", c_int32), ("ckpt_store", c_int32), ("ctas_per_sm", c_int32),
-                ("eager", c_int32)]
+                ("eager", c_int32), ("step_sync", c_int32)]
 
     def as_dict(self):
         return {name: int(getattr(self, name)) for name, _ in self._fields_}

@@ -180,6 +180,7 @@ struct TbParams {
   const TbRec* recs;
   int nrow_max, nrxl_max, tmax;  // nrow_max: staged tap rows of the largest tile
   int adj_coef;          // adjoint: 1 = coefficient tile in shared memory, 0 = read through L1
+  int pair_sync;         // 1: neighbouring warps meet on named barriers after a step, 0: the CTA
   // sources
   const SrcNode* src;    // (nshots, nsrc_max) merged injection nodes
   int nsrc_max;

@@ -118,6 +118,7 @@ struct fdtd_plan {
   int nsrc_max = 1, nsrow_max = 0;
   int nrow_max = 0, nrxl_max = 0;
   int adj_coef = 0;
+  int pair_sync = 0;
   int ckpt_every = 0, nseg = 1;
   size_t field_elems = 0;
   // workspace offsets
@@ -225,6 +226,7 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.recs = reinterpret_cast<const TbRec*>(p->ws + p->o_recs);
   q.nrow_max = p->nrow_max;
   q.adj_coef = p->adj_coef;
+  q.pair_sync = p->pair_sync;
   q.nrxl_max = p->nrxl_max;
   q.tmax = p->tmax;
   q.src = reinterpret_cast<const SrcNode*>(p->ws + p->o_src);
@@ -811,6 +813,13 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   }
   if (t.steps_per_launch < 1 || t.steps_per_launch > 48) { delete p; return fail(FDTD_ERR_UNSUPPORTED, "steps_per_launch must be in [1, 48]"); }
   if (t.ctas_per_sm == 0) t.ctas_per_sm = 1;
+  if (t.step_sync < FDTD_SYNC_AUTO || t.step_sync > FDTD_SYNC_PAIR) { delete p; return fail(FDTD_ERR_INVALID, "bad step_sync"); }
+  if (t.step_sync == FDTD_SYNC_PAIR && t.warps > 16) {
+    delete p;
+    return fail(FDTD_ERR_UNSUPPORTED, "step_sync PAIR needs at most 16 warps (15 named barriers)");
+  }
+  if (t.step_sync == FDTD_SYNC_AUTO) t.step_sync = t.warps <= 16 ? FDTD_SYNC_PAIR : FDTD_SYNC_CTA;
+  p->pair_sync = t.step_sync == FDTD_SYNC_PAIR;
   if (t.ckpt_store < 0 || t.ckpt_store > 2) { delete p; return fail(FDTD_ERR_INVALID, "bad checkpoint storage type"); }
   p->ky = t.rows_per_lane;
   p->nw = t.warps;

@@ -150,6 +150,25 @@ __device__ __forceinline__ void tm_st8(unsigned addr, const unsigned (&v)[8]) {
 __device__ __forceinline__ void tm_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
+// End of a step. Only the warps above and below read the rows a warp published,
+// so with pair_sync each neighbouring pair (j, j+1) meets on its own named
+// barrier j+1 (barrier 0 stays the CTA-wide __syncthreads): the pairs (2i, 2i+1)
+// first, then (2i+1, 2i+2), so that no barrier waits on a chain of others. Warps
+// d apart then drift by up to d steps instead of all waiting for the slowest one
+// every step, which spreads the CTA's bursts of stencil arithmetic over time. The
+// double-buffered exchange stays safe: a warp overwrites the buffer it published
+// two steps earlier only after both neighbours met it at the end of the step
+// that read it.
+__device__ __forceinline__ void step_sync(const TbParams& p, const Ctx& x) {
+  if (!p.pair_sync) {
+    __syncthreads();
+    return;
+  }
+  const int a = x.w | 1, b = (x.w + 1) & ~1;
+  if (a < x.nw) asm volatile("bar.sync %0, 64;" ::"r"(a) : "memory");
+  if (b >= 1 && b < x.nw) asm volatile("bar.sync %0, 64;" ::"r"(b) : "memory");
+}
+
 // Coefficients (c dt)^2 of band row r: from the shared-memory copy of the region
 // or, for an adjoint without room for it, through L1 from global memory; zero
 // outside the domain.
@@ -587,7 +606,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   // ---- publish the band's first and last rows for the next step
   xout[x.w * 64 + x.lane] = opval(P[0]);
   xout[x.w * 64 + 32 + x.lane] = opval(P[KY - 1]);
-  __syncthreads();
+  step_sync(p, x);
 }
 
 // psi_y (new) on the bottom faces of one lane row: decay of the old value plus
@@ -783,7 +802,7 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
   xout[x.w * 64 + x.lane] = opval(P[0]);
   xout[x.w * 64 + 32 + x.lane] = opval(P[KY - 1]);
   pout[x.w * 32 + x.lane] = pyb0;
-  __syncthreads();
+  step_sync(p, x);
 }
 
 template <int KY>
@@ -872,6 +891,7 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x, float 
       if (k + 1 < p.nsteps) substep<KY, MODE, EK>(C, P, p, x, k + 1);
     }
   }
+  if (p.pair_sync) __syncthreads();  // the item's end reads every warp's staged taps
   if (p.nsteps & 1) {
     store_state<KY>(p, x, C, P);
   } else {
