@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 5
+#define FDTD_ABI_VERSION 6
 
 enum {
   FDTD_OK = 0,
@@ -50,8 +50,9 @@ enum { FDTD_STORE_F32 = 0, FDTD_STORE_F16 = 1, FDTD_STORE_BF16 = 2 };
 typedef struct fdtd_grid {
   int32_t ny, nx, pitch;
   double dx, dy, dt;
-  const float* coef; /* device (ny, pitch): (c * dt)^2; with a PML q (c * dt)^2, q = 1 / (1 + a),
-                        a = dt (sigma_x + sigma_y) / 2 */
+  const float* coef; /* device (ny, pitch): b = (c * dt / dy)^2, the update coefficient of the
+                        stencil in units of 1/dy^2 (Q = dy^2 lap, see fdtd_step); with a PML
+                        q b, q = 1 / (1 + a), a = dt (sigma_x + sigma_y) / 2 */
   const float* mur;  /* device, 2 * (2 ny + 2 nx + 8) floats: k_left[ny], k_right[ny],
                         k_bottom[nx], k_top[nx], corner_kx[4], corner_ky[4] (corners
                         in the order (0,0), (0,nx-1), (ny-1,0), (ny-1,nx-1)), then in
@@ -157,7 +158,7 @@ int32_t fdtd_prepare_medium(const double* c, int32_t ny, int32_t nx, int32_t pit
    reference counterpart: the reference has first-order Mur edges only). c is the
    padded medium; the damping grows as sigma_max (depth / cells)^2 with
    sigma_max = 3 max(c) ln(1 / reflection) / (2 cells h) per axis. Writes coef =
-   q (c dt)^2, the Mur table (unused by PML grids) and the PML tables
+   q (c dt / dy)^2, the Mur table (unused by PML grids) and the PML tables
    (device, 4 (nx + ny) floats) that fdtd_grid.pml points to. */
 int32_t fdtd_prepare_medium_pml(const double* c, int32_t ny, int32_t nx, int32_t pitch,
                                 double dt, double dx, double dy, int32_t cells, double reflection,
@@ -171,11 +172,14 @@ int32_t fdtd_prepare_density(const double* c, const double* rho, int32_t ny, int
 
 /* ------------------------------------------------- one-step (plain) kernels */
 
-/* One leapfrog step for n_shots shots, Mur edges included:
-     forward: u_next = 2u - u_old + coef * lap(u) + sources
-     adjoint = 1: u_next = 2u - u_old + lap(coef * u) + sources
+/* One leapfrog step for n_shots shots, Mur edges included. With the stencil in
+   units of 1/dy^2, Q(u) = (u_d + u_u) + ratio (u_l + u_r) - 2 (1 + ratio) u,
+   ratio = dy^2 / dx^2 (Q = dy^2 lap(u), zero beyond the grid), and coef = b =
+   (c dt / dy)^2:
+     forward: u_next = 2u - u_old + coef * Q(u) + sources  (= (c dt)^2 lap(u))
+     adjoint = 1: u_next = 2u - u_old + Q(coef * u) + sources
      adjoint = 2: the same adjoint carried as w = coef * u:
-                  w_next = 2w - w_old + coef * lap(w) + coef * sources, with the
+                  w_next = 2w - w_old + coef * Q(w) + coef * sources, with the
                   Mur edges rescaled by the coef ratios (the fused engine's form)
    Sources: `src_*` are device arrays of shape (n_shots, src_per_shot) (row, col,
    weight, waveform index) and inject w * waveforms[wave * waveform_len + step];

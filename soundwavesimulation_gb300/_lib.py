@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "libfdtd_gb300.so"
-ABI_VERSION = 5
+ABI_VERSION = 6
 
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 

@@ -14,6 +14,22 @@ namespace fdtd {
 
 // ---------------------------------------------------------------- arithmetic
 
+// The update stencil in units of 1/dy^2 (the conv2d kernel of
+// fdtd2d/torch_backend.py:124-132 with zero padding, times dy^2):
+//   Q(u) = (d + u) + ratio (l + r) + qdiag c,  ratio = dy^2 / dx^2,
+//   qdiag = -2 (1 + ratio),  lap(u) = Q(u) / dy^2.
+// The coefficient array holds b = (c dt / dy)^2, rounded once from float64, so the
+// leapfrog u+ = 2u - u- + b Q(u) needs no per-step multiply by 1/dy^2: six float32
+// operations per cell, and one rounding fewer per step than b' lap(u) with
+// b' = (c dt)^2. With dx = dy, ratio = 1 and qdiag = -4 are exact.
+__device__ __forceinline__ float nbrq(float l, float r, float d, float u, float ratio) {
+  return __fmaf_rn(__fadd_rn(l, r), ratio, __fadd_rn(d, u));
+}
+
+__device__ __forceinline__ float lapq(float c, float l, float r, float d, float u, float ratio, float qdiag) {
+  return __fmaf_rn(c, qdiag, nbrq(l, r, d, u, ratio));
+}
+
 // Off-centre part of the 5-point Laplacian, (l + r) / dx^2 + (d + u) / dy^2.
 __device__ __forceinline__ float nbr4(float l, float r, float d, float u, float idx2, float idy2) {
   return __fmaf_rn(__fadd_rn(d, u), idy2, __fmul_rn(__fadd_rn(l, r), idx2));
@@ -26,17 +42,17 @@ __device__ __forceinline__ float lap5(float c, float l, float r, float d, float 
   return __fmaf_rn(c, cdiag, nbr4(l, r, d, u, idx2, idy2));
 }
 
-// Forward leapfrog u+ = 2u - u_old + (c dt)^2 lap(u) (fdtd2d/torch_backend.py:516).
-// 2u - u_old is formed with one rounding (2u is exact). The factor 2 must stay
-// exact: folding it into a per-cell 2 + (c dt)^2 cdiag rounded to float32 shifts
-// every mode's frequency by a fixed relative amount, which accumulates
-// coherently over thousands of steps.
+// Forward leapfrog u+ = 2u - u_old + (c dt)^2 lap(u) (fdtd2d/torch_backend.py:516),
+// as 2u - u_old + b Q(u) (coef = b, lap = Q above). 2u - u_old is formed with one
+// rounding (2u is exact). The factor 2 must stay exact: folding it into a
+// per-cell 2 + b qdiag rounded to float32 shifts every mode's frequency by a
+// fixed relative amount, which accumulates coherently over thousands of steps.
 __device__ __forceinline__ float leap(float c, float p, float coef, float lap) {
   return __fmaf_rn(coef, lap, __fmaf_rn(2.0f, c, -p));
 }
 
-// Adjoint leapfrog 2l - l_old + lap((c dt)^2 l)  (fdtd2d/torch_backend.py:531-532);
-// the coefficient is already inside the Laplacian operand.
+// Adjoint leapfrog 2l - l_old + lap((c dt)^2 l)  (fdtd2d/torch_backend.py:531-532),
+// as 2l - l_old + Q(b l); the coefficient is already inside the operand.
 __device__ __forceinline__ float leap_adj(float c, float p, float lap) {
   return __fadd_rn(__fsub_rn(__fadd_rn(c, c), p), lap);
 }
@@ -46,7 +62,7 @@ __device__ __forceinline__ float mur(float u_in, float k, float un_in, float u_e
   return __fmaf_rn(k, __fsub_rn(un_in, u_edge), u_in);
 }
 
-// The same Mur update for the adjoint carried as w = (c dt)^2 l: with
+// The same Mur update for the adjoint carried as w = coef l: with
 // r = coef_edge / coef_inner, coef_edge * (l_in + k (l_in' - l_edge)) equals
 // r w_in + k (r w_in' - w_edge).
 __device__ __forceinline__ float murw(float r, float w_in, float k, float wn_in, float w_edge) {
@@ -79,8 +95,8 @@ __device__ __forceinline__ float inj_add(float un, float inj) { return __fadd_rn
 //   phi_x_t = -sx phi_x + (sy - sx) du/dx,  phi_y_t = -sy phi_y + (sx - sy) du/dy,
 // with phi on the cell faces at half steps, stored as psi = phi / h: psi_x of cell
 // (y, x) lives on its left face, psi_y on its bottom face. Tables per column
-// (sigma_x at the centre and the left face, the face decay and forcing scale) and
-// per row (the same for y) come from fdtd_prepare_medium_pml; the update factors
+// (sigma_x at the centre and the left face, the face decay and forcing scale, the
+// latter times dy^2) and per row (the same for y) come from fdtd_prepare_medium_pml; the update factors
 // of a cell follow from sigma_x, sigma_y at its centre. Where sigma = 0 every
 // factor is exactly 1 or 2 and psi stays 0, so the update is bit for bit the
 // plain leapfrog (leap above).
@@ -92,8 +108,9 @@ __device__ __forceinline__ float pml_face(float alpha, float psi, float sig_othe
 }
 
 // Factors A = q (2 - dt^2 sx sy) and M = (1 - a) q, with a = dt (sx + sy) / 2 and
-// q = 1 / (1 + a), of the cell update u+ = K (lap + div) + A u - M u-, where the
-// coefficient table holds K = q (c dt)^2.
+// q = 1 / (1 + a), of the cell update u+ = K (Q + div) + A u - M u-, where the
+// coefficient table holds K = q (c dt / dy)^2 and the face fields carry the
+// factor dy^2 of Q (their forcing scale includes it).
 __device__ __forceinline__ void pml_factors(float sxc, float syc, float hdt, float dt2, float& A, float& M) {
   const float a = __fmul_rn(hdt, __fadd_rn(sxc, syc));
   const float q = __frcp_rn(__fadd_rn(1.0f, a));
@@ -106,7 +123,7 @@ __device__ __forceinline__ float pml_div(float pxl, float pxr, float pyb, float 
   return __fadd_rn(__fsub_rn(pxr, pxl), __fsub_rn(pyt, pyb));
 }
 
-// u+ = K (lap + div) + (A u - M u-): the plain leap when A = 2, M = 1, div = 0.
+// u+ = K (Q + div) + (A u - M u-): the plain leap when A = 2, M = 1, div = 0.
 __device__ __forceinline__ float pml_leap(float c, float p, float K, float A, float M, float lap, float div) {
   return __fmaf_rn(K, __fadd_rn(lap, div), __fmaf_rn(A, c, -__fmul_rn(M, p)));
 }
@@ -159,6 +176,13 @@ struct SrcNode {         // one injection node of one shot
   float w[SRC_C];
 };
 
+// Per (tile, thread): the band rows holding receiver tap nodes and the first
+// staged tap row (0x7fffffff without taps); shot-independent, built by the plan.
+struct TbMask {
+  unsigned mask;
+  int base;
+};
+
 struct SrcTap {          // one injection node of one shot inside one tile
   int packed;            // (thread << 8) | (row_in_lane * 4 + column_in_lane)
   int srow;              // staged source row (its float is srow * 4 + column)
@@ -170,12 +194,14 @@ struct TbParams {
   // grid
   int ny, nx, pitch;
   float idx2, idy2, cdiag;
-  const float* coef;     // (c dt)^2
+  float ratio, qdiag;    // the stencil Q in units of 1/dy^2 (see nbrq)
+  const float* coef;     // b = (c dt / dy)^2
   const float* mur;
   // tiling
   const TbTile* tiles;
   int ntiles, nshots, nwarps;
   const TbTap* taps;
+  const TbMask* tmask;   // (ntiles, nwarps * 32)
   const int* rxl;
   const TbRec* recs;
   int nrow_max, nrxl_max, tmax;  // nrow_max: staged tap rows of the largest tile
@@ -228,7 +254,7 @@ struct TbGroup {
 // Dynamic shared-memory carve-up of the temporally blocked kernel; the host
 // sizes the launch with the same function.
 struct TbSmem {
-  size_t coef, lap, g, xch, mur, tap, res, src, mask, base, smask, sbase, pcol, prow, pxch, slots, nslot, total;
+  size_t coef, lap, g, xch, mur, tap, res, src, smask, sbase, pcol, prow, pxch, slots, nslot, total;
 };
 
 __host__ __device__ inline size_t tb_align16(size_t v) { return (v + 15) & ~size_t(15); }
@@ -263,8 +289,6 @@ __host__ __device__ inline TbSmem tb_smem_layout(int nw, int ky, int mode, int n
   // source stage: per step, the 4-cell rows holding this shot's injection nodes
   // (forward and recompute only)
   m.src = off; if (mode != MODE_ADJ) off += size_t(tmax) * (nsrow_max > 0 ? nsrow_max : 1) * 4 * sizeof(float);
-  m.mask = off; off += size_t(nw) * 32 * sizeof(unsigned);
-  m.base = off; off += size_t(nw) * 32 * sizeof(int);
   m.smask = off; off += size_t(nw) * 32 * sizeof(unsigned);
   m.sbase = off; off += size_t(nw) * 32 * sizeof(int);
   // PML grids (slot_cap > 0): the region's column and row tables (one row more,

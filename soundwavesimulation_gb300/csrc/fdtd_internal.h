@@ -38,7 +38,8 @@ size_t tb_group_static_smem();
 struct StepArgs {
   int ny, nx, pitch;
   float idx2, idy2, cdiag;
-  const float* coef;
+  float ratio, qdiag;  // the stencil Q = dy^2 lap (fdtd_device.cuh nbrq)
+  const float* coef;   // b = (c dt / dy)^2
   const float* mur;
   int n_shots;
   const float* u_old;

@@ -61,10 +61,10 @@ __device__ float cell_next(const StepArgs& a, int s, int y, int x) {
     if (a.dense) un = inj_add(un, a.dense[s * plane + i]);
     return un;
   }
-  const float nb = nbr4(operand(a, u, y, x - 1), operand(a, u, y, x + 1), operand(a, u, y - 1, x),
-                        operand(a, u, y + 1, x), a.idx2, a.idy2);
-  const float lap = __fmaf_rn(operand(a, u, y, x), a.cdiag, nb);
-  // adjoint 1: l+ = 2l - l- + lap(coef l); adjoint 2 (w = coef l): the forward form
+  const float nb = nbrq(operand(a, u, y, x - 1), operand(a, u, y, x + 1), operand(a, u, y - 1, x),
+                        operand(a, u, y + 1, x), a.ratio);
+  const float lap = __fmaf_rn(operand(a, u, y, x), a.qdiag, nb);  // Q = dy^2 lap
+  // adjoint 1: l+ = 2l - l- + Q(coef l); adjoint 2 (w = coef l): the forward form
   float un = a.adjoint == 1 ? leap_adj(u[i], uo[i], lap) : leap(u[i], uo[i], a.coef[i], lap);
   if (a.src_per_shot > 0) {
     float acc = 0.f;
@@ -165,7 +165,7 @@ __global__ void step_pml_kernel(const StepArgs a, const float* __restrict__ pml,
   const float* byf = ayf + ny;
   const long long i = (long long)y * P + x;
   const float uc = U(y, x), ul = U(y, x - 1), ur = U(y, x + 1), ud = U(y - 1, x), uu = U(y + 1, x);
-  const float lap = __fmaf_rn(uc, a.cdiag, nbr4(ul, ur, ud, uu, a.idx2, a.idy2));
+  const float lap = __fmaf_rn(uc, a.qdiag, nbrq(ul, ur, ud, uu, a.ratio));  // Q = dy^2 lap
   const float pxl = pml_face(axf[x], px[i], syc[y], sxf[x], bxf[x], __fsub_rn(uc, ul));
   const float pxr = (x + 1 < nx) ? pml_face(axf[x + 1], px[i + 1], syc[y], sxf[x + 1], bxf[x + 1], __fsub_rn(ur, uc)) : 0.f;
   const float pyb = pml_face(ayf[y], py[i], sxc[x], syf[y], byf[y], __fsub_rn(uc, ud));
@@ -197,7 +197,8 @@ __global__ void step_pml_kernel(const StepArgs a, const float* __restrict__ pml,
 
 // PML tables and the scaled coefficients of a padded medium, in one block: the
 // largest speed (for sigma_max), then per column / row sigma at the centre and at
-// the low face with the face decay and forcing scale, then coef = q (c dt)^2.
+// the low face with the face decay and forcing scale (times dy^2), then
+// coef = q (c dt / dy)^2.
 __device__ __forceinline__ double pml_sigma(double xc, int n, int cells, double smax) {
   const double lo = (cells - 0.5) - xc, hi = xc - (n - cells - 0.5);
   double d = lo > hi ? lo : hi;
@@ -230,19 +231,19 @@ __global__ void pml_prepare_kernel(const double* c, int ny, int nx, int pitch, d
     col[i] = (float)sc;
     col[nx + i] = (float)sf;
     col[2 * nx + i] = (float)((1.0 - 0.5 * dt * sf) / (1.0 + 0.5 * dt * sf));
-    col[3 * nx + i] = (float)(dt / (dx * dx * (1.0 + 0.5 * dt * sf)));
+    col[3 * nx + i] = (float)(dt * (dy * dy) / (dx * dx * (1.0 + 0.5 * dt * sf)));  // times dy^2 (Q units)
   }
   for (int j = threadIdx.x; j < ny; j += blockDim.x) {
     const double sc = pml_sigma(j, ny, cells, smy), sf = pml_sigma(j - 0.5, ny, cells, smy);
     row[j] = (float)sc;
     row[ny + j] = (float)sf;
     row[2 * ny + j] = (float)((1.0 - 0.5 * dt * sf) / (1.0 + 0.5 * dt * sf));
-    row[3 * ny + j] = (float)(dt / (dy * dy * (1.0 + 0.5 * dt * sf)));
+    row[3 * ny + j] = (float)(dt / (1.0 + 0.5 * dt * sf));  // dt / dy^2 times dy^2
   }
   for (long long k = threadIdx.x; k < (long long)ny * nx; k += blockDim.x) {
     const int y = (int)(k / nx), x = (int)(k - (long long)y * nx);
     const double q = 1.0 / (1.0 + 0.5 * dt * (pml_sigma(x, nx, cells, smx) + pml_sigma(y, ny, cells, smy)));
-    const double cd = c[k] * dt;
+    const double cd = c[k] * dt / dy;
     coef[(long long)y * pitch + x] = (float)(cd * cd * q);
   }
 }
@@ -397,13 +398,14 @@ __device__ __forceinline__ double mur_k(double c, double dt, double h) {
   return (c * dt - h) / (c * dt + h);
 }
 
-__global__ void coef_kernel(const double* c, int ny, int nx, int pitch, double dt, float* coef) {
+// b = (c dt / dy)^2, rounded once from float64 (the update in units of 1/dy^2).
+__global__ void coef_kernel(const double* c, int ny, int nx, int pitch, double dt, double dy, float* coef) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= pitch || y >= ny) return;
   float v = 0.f;
   if (x < nx) {
-    const double cd = c[(long long)y * nx + x] * dt;
+    const double cd = c[(long long)y * nx + x] * dt / dy;
     v = (float)(cd * cd);
   }
   coef[(long long)y * pitch + x] = v;
@@ -590,7 +592,7 @@ cudaError_t prepare_medium_launch(const double* c, int ny, int nx, int pitch, do
                                   cudaStream_t st) {
   dim3 block(32, 8);
   dim3 grid((pitch + 31) / 32, (ny + 7) / 8);
-  coef_kernel<<<grid, block, 0, st>>>(c, ny, nx, pitch, dt, coef);
+  coef_kernel<<<grid, block, 0, st>>>(c, ny, nx, pitch, dt, dy, coef);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int n = (ny > nx ? ny : nx);

@@ -109,6 +109,7 @@ struct fdtd_plan {
   int ky = 8, nw = 16, tmax = 12, RY = 128;
   std::vector<TbTile> tiles;
   std::vector<TbTap> taps;
+  std::vector<TbMask> tmask;  // (tiles, threads): tap rows and first staged row per thread
   std::vector<int> rxl;
   std::vector<TbRec> recs;
   std::vector<SrcNode> src;       // (n_shots, nsrc_max) merged nodes
@@ -122,7 +123,7 @@ struct fdtd_plan {
   int ckpt_every = 0, nseg = 1;
   size_t field_elems = 0;
   // workspace offsets
-  size_t o_tiles = 0, o_taps = 0, o_rxl = 0, o_recs = 0, o_src = 0, o_stap = 0, o_stap_off = 0;
+  size_t o_tiles = 0, o_taps = 0, o_tmask = 0, o_rxl = 0, o_recs = 0, o_src = 0, o_stap = 0, o_stap_off = 0;
   size_t o_state[2][2] = {{0, 0}, {0, 0}};
   size_t o_adj[2][2] = {{0, 0}, {0, 0}};
   // PML grids: the face fields psi_x, psi_y of the forward and adjoint ping-pong
@@ -215,6 +216,8 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.idx2 = (float)idx2;
   q.idy2 = (float)idy2;
   q.cdiag = (float)(-2.0 * (idx2 + idy2));
+  q.ratio = (float)(idx2 / idy2);
+  q.qdiag = (float)(-2.0 * (1.0 + idx2 / idy2));
   q.coef = g.coef;
   q.mur = g.mur;
   q.tiles = reinterpret_cast<const TbTile*>(p->ws + p->o_tiles);
@@ -222,6 +225,7 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.nshots = p->prob.n_shots;
   q.nwarps = p->nw;
   q.taps = reinterpret_cast<const TbTap*>(p->ws + p->o_taps);
+  q.tmask = reinterpret_cast<const TbMask*>(p->ws + p->o_tmask);
   q.rxl = reinterpret_cast<const int*>(p->ws + p->o_rxl);
   q.recs = reinterpret_cast<const TbRec*>(p->ws + p->o_recs);
   q.nrow_max = p->nrow_max;
@@ -307,13 +311,34 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
 
   p->tiles.clear();
   p->taps.clear();
+  p->tmask.clear();
   p->rxl.clear();
   p->recs.clear();
   p->nrow_max = 0;
   p->nrxl_max = 0;
   std::vector<int> recorded(R, 0);
-  for (const AxisTile& ay : ty) {
-    for (const AxisTile& ax : tx) {
+  // Tiles in decreasing order of cost (Mur edges and corners first, then tiles
+  // with receiver taps, interior tiles last). Items are (tile, shot) pairs dealt
+  // out to the persistent CTAs with a grid stride in this order, so the partial
+  // last round of a launch holds the cheapest items.
+  struct Order { int cost, j, i; };  // indices into ty, tx
+  std::vector<Order> order;
+  for (size_t j = 0; j < ty.size(); ++j)
+    for (size_t i = 0; i < tx.size(); ++i) {
+      const int fy = ty[j].flags, fx = tx[i].flags;
+      const int edges = ((fy & 1) != 0) + ((fy & 2) != 0) + ((fx & 1) != 0) + ((fx & 2) != 0);
+      bool taps = false;
+      for (const auto& nd : nodes) {
+        const int ly = nd.first - ty[j].origin, lx = nd.second - tx[i].origin;
+        if (ly >= 0 && ly < RY && lx >= 0 && lx < RX) { taps = true; break; }
+      }
+      order.push_back({2 * edges + (taps ? 1 : 0), (int)j, (int)i});
+    }
+  std::stable_sort(order.begin(), order.end(), [](const Order& a, const Order& b) { return a.cost > b.cost; });
+  for (const Order& o : order) {
+    {
+      const AxisTile& ay = ty[o.j];
+      const AxisTile& ax = tx[o.i];
       TbTile t;
       std::memset(&t, 0, sizeof(t));
       t.rx0 = ax.origin;
@@ -362,6 +387,8 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
       for (auto& kv : rloc) { kv.second = (int)rx_here.size(); rx_here.push_back(kv.first); }
       t.tap_off = (int)p->taps.size();
       t.ntap = (int)local.size();
+      const size_t mbase = p->tmask.size();
+      p->tmask.resize(mbase + (size_t)p->nw * 32, TbMask{0u, 0x7fffffff});
       std::map<int, int> slot_of_node;  // node id -> staged float (srow * 4 + column)
       t.nrow = 0;
       for (size_t i = 0; i < local.size(); ++i) {
@@ -377,6 +404,9 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
           tp.w[q] = cl[q].second;
         }
         p->taps.push_back(tp);
+        TbMask& mk = p->tmask[mbase + (tp.packed >> 8)];
+        mk.mask |= 1u << ((tp.packed & 255) >> 2);
+        mk.base = std::min(mk.base, tp.srow);
         slot_of_node[local[i].second] = tp.srow * 4 + (tp.packed & 3);
       }
       t.rxl_off = (int)p->rxl.size();
@@ -594,6 +624,8 @@ int32_t fdtd_step_pml(const fdtd_grid* grid, int32_t n_shots, const float* u_old
   a.idx2 = (float)idx2;
   a.idy2 = (float)idy2;
   a.cdiag = (float)(-2.0 * (idx2 + idy2));
+  a.ratio = (float)(idx2 / idy2);
+  a.qdiag = (float)(-2.0 * (1.0 + idx2 / idy2));
   a.coef = grid->coef;
   a.mur = grid->mur;
   a.n_shots = n_shots;
@@ -643,6 +675,8 @@ int32_t step_impl(const fdtd_grid* grid, const fdtd_density* density, int32_t n_
   a.idx2 = (float)idx2;
   a.idy2 = (float)idy2;
   a.cdiag = (float)(-2.0 * (idx2 + idy2));
+  a.ratio = (float)(idx2 / idy2);
+  a.qdiag = (float)(-2.0 * (1.0 + idx2 / idy2));
   a.coef = grid->coef;
   a.mur = grid->mur;
   a.n_shots = n_shots;
@@ -856,6 +890,7 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   size_t off = 0;
   p->o_tiles = off; off = align_up(off + p->tiles.size() * sizeof(TbTile));
   p->o_taps = off; off = align_up(off + std::max<size_t>(1, p->taps.size()) * sizeof(TbTap));
+  p->o_tmask = off; off = align_up(off + p->tmask.size() * sizeof(TbMask));
   p->o_rxl = off; off = align_up(off + std::max<size_t>(1, p->rxl.size()) * sizeof(int));
   p->o_recs = off; off = align_up(off + std::max<size_t>(1, p->recs.size()) * sizeof(TbRec));
   p->o_src = off; off = align_up(off + p->src.size() * sizeof(SrcNode));
@@ -919,6 +954,7 @@ int32_t fdtd_plan_bind(fdtd_plan* p, void* workspace, size_t bytes, void* stream
   const Up ups[] = {
       {p->o_tiles, p->tiles.data(), p->tiles.size() * sizeof(TbTile)},
       {p->o_taps, p->taps.data(), p->taps.size() * sizeof(TbTap)},
+      {p->o_tmask, p->tmask.data(), p->tmask.size() * sizeof(TbMask)},
       {p->o_rxl, p->rxl.data(), p->rxl.size() * sizeof(int)},
       {p->o_recs, p->recs.data(), p->recs.size() * sizeof(TbRec)},
       {p->o_src, p->src.data(), p->src.size() * sizeof(SrcNode)},

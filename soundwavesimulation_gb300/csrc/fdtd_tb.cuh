@@ -82,7 +82,7 @@ struct Ctx {
 };
 
 // Stencil operand of one band row: the field itself in every mode (the adjoint
-// is carried as w = (c dt)^2 l, so its update has the forward's form).
+// is carried as w = coef l, so its update has the forward's form).
 __device__ __forceinline__ float4 opval(const float (&v)[4]) {
   return make_float4(v[0], v[1], v[2], v[3]);
 }
@@ -169,7 +169,7 @@ __device__ __forceinline__ void step_sync(const TbParams& p, const Ctx& x) {
   if (b >= 1 && b < x.nw) asm volatile("bar.sync %0, 64;" ::"r"(b) : "memory");
 }
 
-// Coefficients (c dt)^2 of band row r: from the shared-memory copy of the region
+// Coefficients b = (c dt / dy)^2 of band row r: from the shared-memory copy of the region
 // or, for an adjoint without room for it, through L1 from global memory; zero
 // outside the domain.
 template <int MODE>
@@ -447,10 +447,10 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   float4* xout = x.s_xch + ((k + 1) & 1) * x.nw * 64;
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
   // Paired-lane (f32x2) arithmetic: every element is rounded once, exactly like the
-  // scalar helpers of fdtd_device.cuh, so the values stay bit-identical to the
-  // one-step kernels while one instruction updates two cells.
-  const float2 I2 = make_float2(p.idx2, p.idx2), J2 = make_float2(p.idy2, p.idy2);
-  const float2 D2 = make_float2(p.cdiag, p.cdiag), TWO2 = make_float2(2.0f, 2.0f);
+  // scalar helpers of fdtd_device.cuh (nbrq / lapq / leap), so the values stay
+  // bit-identical to the one-step kernels while one instruction updates two cells.
+  const float2 R2 = make_float2(p.ratio, p.ratio), Q2 = make_float2(p.qdiag, p.qdiag);
+  const float2 J2 = make_float2(p.idy2, p.idy2), TWO2 = make_float2(2.0f, 2.0f);
 
   // ---- stencil over the band, rolling the row above / below
   float4 prv = (x.w > 0) ? xin[(x.w - 1) * 64 + 32 + x.lane] : zero4;
@@ -472,7 +472,8 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
     float rgt = __shfl_down_sync(FULL, cur.x, 1);
     if (lzero) lft = 0.f;
     if (rzero) rgt = 0.f;
-    // nbr4 / lap5 / leap of fdtd_device.cuh on cell pairs (0,1) and (2,3). The
+    // nbrq / lapq / leap of fdtd_device.cuh on cell pairs (0,1) and (2,3): the
+    // stencil Q = dy^2 lap against the coefficient b = (c dt / dy)^2. The
     // left + right sums are scalar: their operands (lft, c0), (c1, c2), (c3, rgt)
     // straddle the register pairs, and a paired add would first need them
     // copied into place (more instructions than the four scalar adds).
@@ -480,16 +481,17 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
     const float2 udB = __fadd2_rn(make_float2(prv.z, prv.w), make_float2(nxt.z, nxt.w));
     const float2 lrA = make_float2(__fadd_rn(lft, cur.y), __fadd_rn(cur.x, cur.z));
     const float2 lrB = make_float2(__fadd_rn(cur.y, cur.w), __fadd_rn(cur.z, rgt));
-    const float2 nA = __ffma2_rn(udA, J2, __fmul2_rn(lrA, I2));
-    const float2 nB = __ffma2_rn(udB, J2, __fmul2_rn(lrB, I2));
+    const float2 nA = __ffma2_rn(lrA, R2, udA);
+    const float2 nB = __ffma2_rn(lrB, R2, udB);
     {
       const float4 co = coefrow<MODE>(p, x, coef4, r);
-      const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), D2, nA);
-      const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), D2, nB);
-      const float l0 = lA.x, l1 = lA.y, l2 = lB.x, l3 = lB.y;
+      const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), Q2, nA);
+      const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), Q2, nB);
       if (MODE == MODE_REC) {
-        // whole owned rows in one 16-byte store; the per-column form only in the
-        // rare warps holding a lane that owns part of its columns
+        // lap = Q / dy^2, whole owned rows in one 16-byte store; the per-column
+        // form only in the rare warps holding a lane that owns part of its columns
+        const float2 gA = __fmul2_rn(lA, J2), gB = __fmul2_rn(lB, J2);
+        const float l0 = gA.x, l1 = gA.y, l2 = gB.x, l3 = gB.y;
         float* dst = segrow + (long long)r * p.pitch;
         if ((x.rfull >> r) & 1u) {
           *reinterpret_cast<float4*>(dst) = make_float4(l0, l1, l2, l3);
@@ -637,8 +639,8 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
   const float4* pin = x.s_pxch + (k & 1) * x.nw * 32;
   float4* pout = x.s_pxch + ((k + 1) & 1) * x.nw * 32;
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
-  const float2 I2 = make_float2(p.idx2, p.idx2), J2 = make_float2(p.idy2, p.idy2);
-  const float2 D2 = make_float2(p.cdiag, p.cdiag);
+  const float2 R2 = make_float2(p.ratio, p.ratio), Q2 = make_float2(p.qdiag, p.qdiag);
+  const float2 J2 = make_float2(p.idy2, p.idy2);
   const float4 sxc = reinterpret_cast<const float4*>(x.s_pcol)[x.lane];
   const float4 sxf = reinterpret_cast<const float4*>(x.s_pcol + RX)[x.lane];
   const float4 axf = reinterpret_cast<const float4*>(x.s_pcol + 2 * RX)[x.lane];
@@ -686,24 +688,25 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
       slot[r] = pxl;
       slot[KY + r] = pyb;
     }
-    // the Laplacian exactly as substep computes it
+    // the stencil Q = dy^2 lap exactly as substep computes it
     const float2 udA = __fadd2_rn(make_float2(prv.x, prv.y), make_float2(nxt.x, nxt.y));
     const float2 udB = __fadd2_rn(make_float2(prv.z, prv.w), make_float2(nxt.z, nxt.w));
     const float2 lrA = make_float2(__fadd_rn(lft, cur.y), __fadd_rn(cur.x, cur.z));
     const float2 lrB = make_float2(__fadd_rn(cur.y, cur.w), __fadd_rn(cur.z, rgt));
-    const float2 nA = __ffma2_rn(udA, J2, __fmul2_rn(lrA, I2));
-    const float2 nB = __ffma2_rn(udB, J2, __fmul2_rn(lrB, I2));
-    const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), D2, nA);
-    const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), D2, nB);
+    const float2 nA = __ffma2_rn(lrA, R2, udA);
+    const float2 nB = __ffma2_rn(lrB, R2, udB);
+    const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), Q2, nA);
+    const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), Q2, nB);
     if (MODE == MODE_REC) {
+      const float2 gA = __fmul2_rn(lA, J2), gB = __fmul2_rn(lB, J2);  // lap = Q / dy^2
       float* dst = segrow + (long long)r * p.pitch;
       if ((x.rfull >> r) & 1u) {
-        *reinterpret_cast<float4*>(dst) = make_float4(lA.x, lA.y, lB.x, lB.y);
+        *reinterpret_cast<float4*>(dst) = make_float4(gA.x, gA.y, gB.x, gB.y);
       } else if ((x.rpart >> r) & 1u) {
-        if (x.own_cols & 1u) dst[0] = lA.x;
-        if (x.own_cols & 2u) dst[1] = lA.y;
-        if (x.own_cols & 4u) dst[2] = lB.x;
-        if (x.own_cols & 8u) dst[3] = lB.y;
+        if (x.own_cols & 1u) dst[0] = gA.x;
+        if (x.own_cols & 2u) dst[1] = gA.y;
+        if (x.own_cols & 4u) dst[2] = gB.x;
+        if (x.own_cols & 8u) dst[3] = gB.y;
       }
     }
     const float4 co = coefrow<MODE>(p, x, coef4, r);
@@ -875,12 +878,11 @@ __device__ __forceinline__ void prefetch_state(const TbParams& p, const Ctx& x, 
   }
 }
 
+// The T steps of one item; the item setup has published the band's first and
+// last rows and met the whole CTA.
 template <int KY, int MODE, int EK>
 __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x, float (&P)[KY][4], float (&C)[KY][4]) {
-  x.s_xch[x.w * 64 + x.lane] = opval(C[0]);
-  x.s_xch[x.w * 64 + 32 + x.lane] = opval(C[KY - 1]);
   if (MODE == MODE_ADJ && x.own_rows && x.own_cols && p.n0 >= 1) prefetch_lap<KY>(p, x, p.n0);
-  __syncthreads();
 
   for (int k = 0; k < p.nsteps; k += 2) {
     if constexpr (EK == EK_PML) {
@@ -891,7 +893,11 @@ __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x, float 
       if (k + 1 < p.nsteps) substep<KY, MODE, EK>(C, P, p, x, k + 1);
     }
   }
-  if (p.pair_sync) __syncthreads();  // the item's end reads every warp's staged taps
+  // the item's end reads every warp's staged taps; with CTA-wide step barriers
+  // the last step's barrier is this one. Past it no thread reads a shared buffer
+  // that the next item's setup writes before its own CTA barrier, so an item
+  // needs no barrier after its traces and stores.
+  if (p.pair_sync) __syncthreads();
   if (p.nsteps & 1) {
     store_state<KY>(p, x, C, P);
   } else {
@@ -926,8 +932,6 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
   const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef, p.nsrow_max,
                                   p.slot_cap);
   float* s_res = reinterpret_cast<float*>(smem + L.res);
-  unsigned* s_mask = reinterpret_cast<unsigned*>(smem + L.mask);
-  int* s_base = reinterpret_cast<int*>(smem + L.base);
   unsigned* s_smask = reinterpret_cast<unsigned*>(smem + L.smask);
   int* s_sbase = reinterpret_cast<int*>(smem + L.sbase);
   {
@@ -1030,13 +1034,11 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
         else x.s_mur[i] = src ? __ldg(src) : 0.f;
       }
     }
-    s_mask[x.tid] = 0u;
-    s_base[x.tid] = 0x7fffffff;
-    s_smask[x.tid] = 0u;
-    s_sbase[x.tid] = 0x7fffffff;
     // this shot's injection nodes inside the region (sorted by thread, row, column)
     const int so = (MODE != MODE_ADJ) ? __ldg(p.stap_off + s * p.ntiles + ti) : 0;
     const int ns = (MODE != MODE_ADJ) ? __ldg(p.stap_off + s * p.ntiles + ti + 1) - so : 0;
+    s_smask[x.tid] = 0u;  // (read back by this thread only; other threads' atomics follow a barrier)
+    s_sbase[x.tid] = 0x7fffffff;
     if (MODE != MODE_ADJ && ns > 0) {
       // staged source rows start at zero: cells without a node add nothing
       const int nrows = p.stap[so + ns - 1].srow + 1;
@@ -1057,7 +1059,9 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
         s_res[j * p.tmax + k] = __ldg(p.residual + ((long long)s * p.nrx + rg) * p.nt + (p.n0 - k));
       }
     }
-    __syncthreads();
+    // the cleared stages, residual samples and PML tables before their cooperative
+    // fills below (items without sources, injections or PML cells skip it)
+    if (MODE == MODE_ADJ || ns > 0 || pml_tile) __syncthreads();
     bool pml_warp = false;
     if (PML && pml_tile) {
       // a thread holding a layer cell (sigma_x > 0 in one of its columns or
@@ -1091,13 +1095,8 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
         }
       }
     }
-    // per thread: which band rows hold tap nodes / source nodes, and the first
-    // staged row of each; the source values of every step go to the stage
-    for (int i = x.tid; i < t.ntap; i += nthr) {
-      const TbTap& tp = p.taps[t.tap_off + i];
-      atomicOr(&s_mask[tp.packed >> 8], 1u << ((tp.packed & 255) >> 2));
-      atomicMin(&s_base[tp.packed >> 8], tp.srow);
-    }
+    // per thread: which band rows hold source nodes, and the first staged row;
+    // the source values of every step go to the stage
     for (int i = x.tid; i < ns; i += nthr) {
       const SrcTap st = p.stap[so + i];
       atomicOr(&s_smask[st.packed >> 8], 1u << ((st.packed & 255) >> 2));
@@ -1118,11 +1117,6 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
       }
       x.s_src[(k * p.nsrow_max + st.srow) * 4 + (st.packed & 3)] = acc;
     }
-    if (ASYNC_FILL) {  // the coefficient and Mur table copies
-      cp_async_commit();
-      cp_async_wait_all();
-    }
-    __syncthreads();
     if (MODE == MODE_ADJ) {
       for (int i = x.tid; i < t.ntap * p.nsteps; i += nthr) {
         const int ti2 = i / p.nsteps, k = i - ti2 * p.nsteps;
@@ -1140,11 +1134,21 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
             __fmul_rn(__ldg(p.coef + (long long)gy * p.pitch + gx), acc);
       }
     }
-    x.mask = s_mask[x.tid];
-    x.base = s_base[x.tid];
+    // this thread's band rows holding receiver tap nodes and its first staged tap
+    // row (shot-independent, from the plan), and the band's first and last rows
+    // for the first step
+    const int2 tmk = __ldg(reinterpret_cast<const int2*>(p.tmask) + (long long)ti * nthr + x.tid);
+    x.s_xch[x.w * 64 + x.lane] = opval(C[0]);
+    x.s_xch[x.w * 64 + 32 + x.lane] = opval(C[KY - 1]);
+    if (ASYNC_FILL) {  // the coefficient and Mur table copies
+      cp_async_commit();
+      cp_async_wait_all();
+    }
+    __syncthreads();
+    x.mask = (unsigned)tmk.x;
+    x.base = tmk.y;
     x.smask = s_smask[x.tid];
     x.sbase = s_sbase[x.tid];
-    // run_item publishes the exchange rows and synchronises before the first step
 
     // Edge code only in warps with edge cells: every warp of a tile holding the
     // left or right edge (column 0 / nx-1 and the padding columns sit in every
@@ -1233,7 +1237,6 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
         }
       }
     }
-    __syncthreads();
   }
 }
 

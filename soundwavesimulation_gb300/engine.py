@@ -46,7 +46,7 @@ def ptr(t) -> int:
 
 
 class DeviceMedium:
-    """Float32 coefficients (c dt)^2 and Mur edge coefficients of one grid.
+    """Float32 update coefficients (c dt / dy)^2 and Mur edge coefficients of one grid.
 
     With ``pml_cells`` > 0 the grid is padded by a PML layer of that many cells on
     every side (the medium extended with its edge values), which replaces the Mur

@@ -205,7 +205,7 @@ class _Rotation:
                                  ptr(self.buf[self.inx]), n_src, ptr(rows), ptr(cols), ptr(w), ptr(wave),
                                  ptr(value), 1, 0, ptr(dense), int(adjoint), stream)
         if adjoint == 1:
-            raise ValueError("a PML grid carries the adjoint as w = (c dt)^2 l (adjoint=2)")
+            raise ValueError("a PML grid carries the adjoint as w = coef l (adjoint=2)")
         a, b = self.psi[self.ps], self.psi[self.ps ^ 1]
         return lib.fdtd_step_pml(ctypes.byref(grid), n_shots, ptr(self.buf[self.io]), ptr(self.buf[self.ic]),
                                  ptr(self.buf[self.inx]), ptr(a[0]), ptr(a[1]), ptr(b[0]), ptr(b[1]), n_src,
