@@ -231,7 +231,7 @@ struct TbParams {
   int seg_base;          // step held in segment slot 0
   const float* residual;
   double* grad;
-  double scale;
+  double scale;          // adjoint: dt^2 / dy^2 (the stream holds Q = dy^2 lap), applied per pass
   // PML (pml != nullptr): tables, update constants dt / 2 and dt^2, the face
   // fields psi_x / psi_y in and out (nshots, ny, pitch), and the per-CTA capacity
   // of thread slots holding a thread's face fields in shared memory

@@ -87,6 +87,9 @@ cudaError_t gather_launch(int ny, int pitch, int n_shots, const float* fields, i
 cudaError_t scatter_launch(int ny, int pitch, int n_shots, int n_nodes, const int32_t* nodes,
                            const float* w, const float* res, long long shot_stride,
                            long long rx_stride, float* dense, cudaStream_t st);
+// g[i] += scale graw[i] / coef[i] (nothing where coef is 0), float64, n elements.
+cudaError_t grad_divide_launch(const double* graw, const float* coef, double scale, double* g, long long n,
+                               cudaStream_t st);
 cudaError_t image_launch(int ny, int nx, int pitch, float idx2, float idy2, float cdiag,
                          int n_shots, const float* adj, const float* fwd, double scale,
                          const float* coef_div, double* g, cudaStream_t st);

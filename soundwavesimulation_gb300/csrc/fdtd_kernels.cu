@@ -394,6 +394,15 @@ __global__ void image_kernel(int ny, int nx, int pitch, float idx2, float idy2, 
   g[(long long)y * pitch + x] += a * scale;
 }
 
+// The fused adjoint's gradient: its float64 imaging sums of w Q (w = coef l), scaled
+// and divided by coef once per pass.
+__global__ void grad_divide_kernel(const double* graw, const float* coef, double scale, double* g, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float c = coef[i];
+  if (c != 0.f) g[i] += scale * graw[i] / (double)c;
+}
+
 __device__ __forceinline__ double mur_k(double c, double dt, double h) {
   return (c * dt - h) / (c * dt + h);
 }
@@ -574,6 +583,14 @@ cudaError_t scatter_launch(int ny, int pitch, int n_shots, int n_nodes, const in
   dim3 grid((n_nodes + 127) / 128, n_shots);
   scatter_kernel<<<grid, 128, 0, st>>>(pitch, (long long)ny * pitch, n_shots, n_nodes, nodes, w,
                                        res, shot_stride, rx_stride, dense);
+  return cudaGetLastError();
+}
+
+cudaError_t grad_divide_launch(const double* graw, const float* coef, double scale, double* g, long long n,
+                               cudaStream_t st) {
+  const int threads = 256;
+  const long long blocks = (n + threads - 1) / threads;
+  grad_divide_kernel<<<(unsigned)blocks, threads, 0, st>>>(graw, coef, scale, g, n);
   return cudaGetLastError();
 }
 

@@ -132,7 +132,7 @@ struct fdtd_plan {
   size_t o_psi[2][2] = {{0, 0}, {0, 0}};
   size_t o_apsi[2][2] = {{0, 0}, {0, 0}};
   size_t o_ckpsi = 0;
-  size_t o_ckpt = 0, ckpt_elem_bytes = 4, o_scales = 0, o_seg = 0;
+  size_t o_ckpt = 0, ckpt_elem_bytes = 4, o_scales = 0, o_seg = 0, o_graw = 0;
   size_t total = 0;
   size_t smem[3] = {0, 0, 0};
   // binding
@@ -915,6 +915,9 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
     p->o_ckpt = off; off = align_up(off + nck * p->field_elems * p->ckpt_elem_bytes);
     p->o_scales = off; off = align_up(off + nck * 2 * problem->n_shots * sizeof(float) + 16);
     p->o_seg = off; off = align_up(off + (size_t)p->ckpt_every * fb);
+    // the adjoint's imaging sums sum w Q dt^2 / dy^2 (w = coef l), float64 (ny, pitch),
+    // divided by coef once per pass into the caller's gradient
+    p->o_graw = off; off = align_up(off + (size_t)g.ny * g.pitch * sizeof(double));
   }
   p->total = off;
   *out = p;
@@ -1049,7 +1052,7 @@ int32_t run_graphed(fdtd_plan* p, fdtd_plan::Graph& g, const void* const (&key)[
 
 // One stream operation of a pass: a temporally blocked launch or a helper.
 struct Op {
-  enum Kind { LAUNCH, MEMSET, QUANT, DEQUANT } kind = LAUNCH;
+  enum Kind { LAUNCH, MEMSET, QUANT, DEQUANT, DIVIDE } kind = LAUNCH;
   int mode = 0;
   TbParams q;
   void* dst = nullptr;
@@ -1061,6 +1064,7 @@ struct Op {
   int n_shots = 0;
   long long per_shot = 0;
   int store = 0;
+  double scale = 1.0;
 };
 
 int32_t exec_helper(const Op& op, cudaStream_t st) {
@@ -1072,6 +1076,9 @@ int32_t exec_helper(const Op& op, cudaStream_t st) {
   else if (op.kind == Op::DEQUANT)
     e = dequantize_launch(op.src, op.cscales, op.aux, static_cast<float*>(op.dst), op.n_shots, op.per_shot,
                           op.store, st);
+  else if (op.kind == Op::DIVIDE)
+    e = grad_divide_launch(static_cast<const double*>(op.src), op.aux, op.scale, static_cast<double*>(op.dst),
+                           op.per_shot, st);
   return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "pass helper");
 }
 
@@ -1117,6 +1124,17 @@ struct Sink {
     op.n_shots = n_shots;
     op.per_shot = per_shot;
     op.store = store;
+    return emit(op);
+  }
+  // dst[i] += scale src[i] / coef[i] (nothing where coef is zero), float64, n elements
+  int32_t divide(const double* src, const float* coef, double scale, double* dst, long long n) {
+    Op op;
+    op.kind = Op::DIVIDE;
+    op.src = src;
+    op.aux = coef;
+    op.scale = scale;
+    op.dst = dst;
+    op.per_shot = n;
     return emit(op);
   }
   int32_t dequant(const void* src, const float* scales, const float* base, float* dst, int n_shots,
@@ -1220,11 +1238,17 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Si
   if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_apsi[0][0], fb);
   if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_apsi[0][1], fb);
   if (rc0) return rc0;
+  double* graw = reinterpret_cast<double*>(p->ws + p->o_graw);
+  const long long cells = (long long)p->prob.grid.ny * p->prob.grid.pitch;
+  rc0 = k.memset(graw, (size_t)cells * sizeof(double));
+  if (rc0) return rc0;
   TbParams q;
   fill_params(p, q);
   q.residual = residual;
-  q.grad = grad_c2;
-  q.scale = p->prob.grid.dt * p->prob.grid.dt;
+  q.grad = graw;
+  // the segment buffer holds Q = dy^2 lap(u^{n-1}) (the recompute's stencil value):
+  // dt^2 lap = dt^2 Q / dy^2
+  q.scale = p->prob.grid.dt * p->prob.grid.dt / (p->prob.grid.dy * p->prob.grid.dy);
   q.seg = fptr(p, p->o_seg);
   const int nt = p->prob.n_steps, T = p->tmax, C = p->ckpt_every;
   int adj_in = 0;
@@ -1325,7 +1349,9 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Si
       adj_in = out;
     }
   }
-  return FDTD_OK;
+  // grad_c2 += dt^2 lap-imaging = (dt^2 / dy^2) (sum w Q) / coef: the w = coef l form
+  // divided out once
+  return k.divide(graw, p->prob.grid.coef, q.scale, grad_c2, cells);
 }
 
 // ---- several plans in shared launches (uneven batches: grids of different

@@ -200,6 +200,17 @@ __device__ __forceinline__ void prefetch_lap(const TbParams& p, const Ctx& x, in
   cp_async_commit();
 }
 
+// float32 -> float64 with integer instructions (exact for normal numbers and
+// infinities; subnormal values, never reached by the imaging sums, become zero),
+// which keeps the flush off GB300's narrow float64 pipe.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  unsigned long long b = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e != 0u) b |= ((unsigned long long)(e == 0xFFu ? 0x7FFu : e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)b);
+}
+
 // Mur edges and corners, in registers (plus shuffles across one lane boundary).
 // The tiler places rows 0/1 and ny-2/ny-1 in one band and column 0 at lane 0, c = 0.
 // Cells outside the domain need no per-step treatment: they are loaded as zero
@@ -450,7 +461,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   // scalar helpers of fdtd_device.cuh (nbrq / lapq / leap), so the values stay
   // bit-identical to the one-step kernels while one instruction updates two cells.
   const float2 R2 = make_float2(p.ratio, p.ratio), Q2 = make_float2(p.qdiag, p.qdiag);
-  const float2 J2 = make_float2(p.idy2, p.idy2), TWO2 = make_float2(2.0f, 2.0f);
+  const float2 TWO2 = make_float2(2.0f, 2.0f);
 
   // ---- stencil over the band, rolling the row above / below
   float4 prv = (x.w > 0) ? xin[(x.w - 1) * 64 + 32 + x.lane] : zero4;
@@ -488,10 +499,10 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
       const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), Q2, nA);
       const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), Q2, nB);
       if (MODE == MODE_REC) {
-        // lap = Q / dy^2, whole owned rows in one 16-byte store; the per-column
-        // form only in the rare warps holding a lane that owns part of its columns
-        const float2 gA = __fmul2_rn(lA, J2), gB = __fmul2_rn(lB, J2);
-        const float l0 = gA.x, l1 = gA.y, l2 = gB.x, l3 = gB.y;
+        // Q = dy^2 lap (the adjoint's flush scale carries the 1 / dy^2), whole
+        // owned rows in one 16-byte store; the per-column form only in the rare
+        // warps holding a lane that owns part of its columns
+        const float l0 = lA.x, l1 = lA.y, l2 = lB.x, l3 = lB.y;
         float* dst = segrow + (long long)r * p.pitch;
         if ((x.rfull >> r) & 1u) {
           *reinterpret_cast<float4*>(dst) = make_float4(l0, l1, l2, l3);
@@ -640,7 +651,6 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
   float4* pout = x.s_pxch + ((k + 1) & 1) * x.nw * 32;
   const float4* coef4 = reinterpret_cast<const float4*>(x.s_coef) + (x.w * KY) * 32 + x.lane;
   const float2 R2 = make_float2(p.ratio, p.ratio), Q2 = make_float2(p.qdiag, p.qdiag);
-  const float2 J2 = make_float2(p.idy2, p.idy2);
   const float4 sxc = reinterpret_cast<const float4*>(x.s_pcol)[x.lane];
   const float4 sxf = reinterpret_cast<const float4*>(x.s_pcol + RX)[x.lane];
   const float4 axf = reinterpret_cast<const float4*>(x.s_pcol + 2 * RX)[x.lane];
@@ -698,7 +708,7 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
     const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), Q2, nA);
     const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), Q2, nB);
     if (MODE == MODE_REC) {
-      const float2 gA = __fmul2_rn(lA, J2), gB = __fmul2_rn(lB, J2);  // lap = Q / dy^2
+      const float2 gA = lA, gB = lB;  // Q = dy^2 lap, as substep stores it
       float* dst = segrow + (long long)r * p.pitch;
       if ((x.rfull >> r) & 1u) {
         *reinterpret_cast<float4*>(dst) = make_float4(gA.x, gA.y, gB.x, gB.y);
@@ -1222,18 +1232,14 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
         for (int h = 0; h < 2; ++h) {
           const int r = r0 + h;
           if (!x.own_cols || !((x.own_rows >> r) & 1u)) continue;
-          // the tile summed w * lap with w = coef * l: divide by coef once here, in
-          // float32 (GB300's float64 pipe is ~64x slower); only the cross-item sum
-          // (the atomic) is float64
-          const float4 co = ldg4(x.gcoef + (long long)r * p.pitch);
-          const float sc = (float)p.scale;
-          const float g0 = __uint_as_float(v[4 * h]), g1 = __uint_as_float(v[4 * h + 1]);
-          const float g2 = __uint_as_float(v[4 * h + 2]), g3 = __uint_as_float(v[4 * h + 3]);
+          // the tile summed w * Q over the launch's steps (w = coef * l): the
+          // cross-item sum is float64 (the widening is exact and takes integer
+          // instructions, the sum is an L2 atomic), and the scale dt^2 / dy^2 and
+          // the division by coef wait for the end of the pass (once per cell)
           double* gd = p.grad + (long long)(x.y0 + r) * p.pitch + x.xb;
-          if (x.own_cols & 1u) atomicAdd(gd + 0, (double)(__fdiv_rn(g0, co.x) * sc));
-          if (x.own_cols & 2u) atomicAdd(gd + 1, (double)(__fdiv_rn(g1, co.y) * sc));
-          if (x.own_cols & 4u) atomicAdd(gd + 2, (double)(__fdiv_rn(g2, co.z) * sc));
-          if (x.own_cols & 8u) atomicAdd(gd + 3, (double)(__fdiv_rn(g3, co.w) * sc));
+#pragma unroll
+          for (int c = 0; c < 4; ++c)
+            if ((x.own_cols >> c) & 1u) atomicAdd(gd + c, widen(__uint_as_float(v[4 * h + c])));
         }
       }
     }
