@@ -14,8 +14,9 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-SOURCES = ("csrc/fdtd_kernels.cu", "csrc/fdtd_tb.cu", "csrc/fdtd_tb_pml.cu", "csrc/fdtd_plan.cpp",
-           "csrc/fdtd_noalloc.cu", "csrc/fdtd_optim.cu", "csrc/fdtd_autotune.cpp")
+SOURCES = ("csrc/fdtd_kernels.cu", "csrc/fdtd_tb.cu", "csrc/fdtd_tb_adj.cu", "csrc/fdtd_tb_pml.cu",
+           "csrc/fdtd_tb_pml_adj.cu", "csrc/fdtd_plan.cpp", "csrc/fdtd_noalloc.cu", "csrc/fdtd_optim.cu",
+           "csrc/fdtd_autotune.cpp")
 HEADERS = ("csrc/fdtd_device.cuh", "csrc/fdtd_internal.h", "csrc/fdtd_tb.cuh")
 LIB = HERE / "libfdtd_gb300.so"
 BUILD = HERE / "_build"

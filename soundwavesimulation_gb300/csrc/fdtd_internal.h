@@ -29,7 +29,7 @@ cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem
 // PML family for pml).
 cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem, bool pml);
 // One launch over the items of several plans (same rows per lane and warps).
-cudaError_t tb_group_launch(const TbGroup& g, int ky, int nwarps, int mode, int grid, size_t smem,
+cudaError_t tb_group_launch(const TbGroup& g, int ky, int nwarps, int mode, bool adj_coef, int grid, size_t smem,
                             cudaStream_t st);
 // Static shared memory of the grouped kernel (its copy of one plan's parameters).
 size_t tb_group_static_smem();

@@ -270,10 +270,14 @@ int32_t build_tables(fdtd_plan* p, const fdtd_problem* prob) {
   const fdtd_grid& g = prob->grid;
   const int ny = g.ny, nx = g.nx, KY = p->ky, RY = p->RY;
   const int halo = p->tmax + 1;
+  // gradient plans: the x halo rounded up to whole lanes (4 columns), so that every
+  // interior ownership boundary falls between lanes and the recompute stores its
+  // Laplacian stream as whole 16-byte rows
+  const int halo_x = p->for_gradient ? (halo + 3) / 4 * 4 : halo;
   p->pml = g.pml ? g.pml_cells : 0;
   p->slot_cap = 0;
   std::vector<AxisTile> tx, ty;
-  std::string err = tile_axis(nx, RX, 4, halo, 0, tx);
+  std::string err = tile_axis(nx, RX, 4, halo_x, 0, tx);
   if (!err.empty()) return fail(FDTD_ERR_UNSUPPORTED, "x tiling: " + err);
   err = tile_axis(ny, RY, 1, halo, KY, ty);
   if (!err.empty()) return fail(FDTD_ERR_UNSUPPORTED, "y tiling: " + err);
@@ -1462,9 +1466,11 @@ int32_t group_run(fdtd_plan* const* plans, int n, void* workspace, size_t bytes,
     }
     size_t smem = 0;
     int items = 0;
+    bool adj_coef = true;  // every member keeps its adjoint coefficient tile in shared memory
     for (auto& mb : a.members) {
       smem = std::max(smem, plans[mb.first]->smem[a.mode]);
       items += plans[mb.first]->prob.n_shots * (int)plans[mb.first]->tiles.size();
+      adj_coef = adj_coef && plans[mb.first]->adj_coef;
     }
     if (smem + tb_group_static_smem() > SMEM_LIMIT) return fail(FDTD_ERR_UNSUPPORTED, "group: shared memory need exceeds 227 KB");
     TbGroup g;
@@ -1473,7 +1479,7 @@ int32_t group_run(fdtd_plan* const* plans, int n, void* workspace, size_t bytes,
     g.nplans = (int)a.members.size();
     g.nitems = items;
     const int grid = std::max(1, std::min(items, plans[0]->sm_count * std::max(1, plans[0]->tun.ctas_per_sm)));
-    e = tb_group_launch(g, plans[0]->ky, plans[0]->nw, a.mode, grid, smem, st);
+    e = tb_group_launch(g, plans[0]->ky, plans[0]->nw, a.mode, adj_coef, grid, smem, st);
     if (e != cudaSuccess) return cuda_fail(e, "grouped kernel launch");
     pk += a.members.size();
     ok += a.members.size() + 1;

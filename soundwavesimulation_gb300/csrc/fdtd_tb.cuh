@@ -62,7 +62,8 @@ struct Ctx {
   int rx0, ry0, flags;
   int y0, xb;               // global row of this thread's r = 0, column of c = 0
   unsigned own_rows, own_cols;
-  unsigned rfull, rpart;    // owned band rows of a thread owning all / some of its 4 columns
+  unsigned rfull;           // recompute: owned band rows whose 4-cell row it stores (it owns every
+                            // column of the row that lies inside the grid)
   unsigned mask, smask;     // band rows holding receiver taps / source nodes
   unsigned rowvalid;        // band rows inside the domain (adjoint coefficient loads)
   int base, sbase;          // first staged tap row / source row of this thread
@@ -172,9 +173,9 @@ __device__ __forceinline__ void step_sync(const TbParams& p, const Ctx& x) {
 // Coefficients b = (c dt / dy)^2 of band row r: from the shared-memory copy of the region
 // or, for an adjoint without room for it, through L1 from global memory; zero
 // outside the domain.
-template <int MODE>
+template <int MODE, bool CS>
 __device__ __forceinline__ float4 coefrow(const TbParams& p, const Ctx& x, const float4* coef4, int r) {
-  if (MODE != MODE_ADJ || p.adj_coef) return coef4[r * 32];
+  if (MODE != MODE_ADJ || CS) return coef4[r * 32];
   if (!((x.rowvalid >> r) & 1u)) return make_float4(0.f, 0.f, 0.f, 0.f);
   return ldg4(x.gcoef + (long long)r * p.pitch);
 }
@@ -209,6 +210,44 @@ __device__ __forceinline__ double widen(float f) {
   unsigned long long b = (unsigned long long)(u & 0x80000000u) << 32;
   if (e != 0u) b |= ((unsigned long long)(e == 0xFFu ? 0x7FFu : e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
   return __longlong_as_double((long long)b);
+}
+
+// Imaging of this thread's band: the gradient tile in tensor memory += F times the
+// Laplacian tile that the previous step streamed into shared memory (cp.async), one
+// load-wait-store round trip per row pair, all four columns of a row (a cell this
+// thread does not own sums whatever its slot holds, and is never flushed). FULL: the
+// warp owns every row of its band (no per-pair test). Warp-uniform: the caller
+// checks own_rows.
+template <int KY, bool FULL>
+__device__ __forceinline__ void image_band(const Ctx& x, const float (&F)[KY][4]) {
+  cp_async_wait_all();
+  __syncwarp();  // the tensor-memory instructions need the whole warp converged
+  tm_wait_st();
+  const float4* l4 = reinterpret_cast<const float4*>(x.s_lap) + (x.w * KY) * 32 + x.lane;
+#pragma unroll
+  for (int r = 0; r < KY; r += 2) {
+    if (FULL || ((x.own_rows >> r) & 3u)) {
+      unsigned v[8];
+      tm_ld8(x.tm + 4 * r, v);
+      const float4 la = l4[r * 32];
+      const float4 lb = l4[(r + 1) * 32];
+      tm_wait_ld();
+      float2 g;
+      g = __ffma2_rn(make_float2(F[r][0], F[r][1]), make_float2(la.x, la.y),
+                     make_float2(__uint_as_float(v[0]), __uint_as_float(v[1])));
+      v[0] = __float_as_uint(g.x); v[1] = __float_as_uint(g.y);
+      g = __ffma2_rn(make_float2(F[r][2], F[r][3]), make_float2(la.z, la.w),
+                     make_float2(__uint_as_float(v[2]), __uint_as_float(v[3])));
+      v[2] = __float_as_uint(g.x); v[3] = __float_as_uint(g.y);
+      g = __ffma2_rn(make_float2(F[r + 1][0], F[r + 1][1]), make_float2(lb.x, lb.y),
+                     make_float2(__uint_as_float(v[4]), __uint_as_float(v[5])));
+      v[4] = __float_as_uint(g.x); v[5] = __float_as_uint(g.y);
+      g = __ffma2_rn(make_float2(F[r + 1][2], F[r + 1][3]), make_float2(lb.z, lb.w),
+                     make_float2(__uint_as_float(v[6]), __uint_as_float(v[7])));
+      v[6] = __float_as_uint(g.x); v[7] = __float_as_uint(g.y);
+      tm_st8(x.tm + 4 * r, v);
+    }
+  }
 }
 
 // Mur edges and corners, in registers (plus shuffles across one lane boundary).
@@ -449,7 +488,7 @@ __device__ __forceinline__ void boundary(float (&P)[KY][4], const float (&C)[KY]
   }
 }
 
-template <int KY, int MODE, int EK>
+template <int KY, int MODE, int EK, bool CS>
 __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
                                         const TbParams& p, const Ctx& x, int k) {
   const int n = (MODE == MODE_ADJ) ? p.n0 - k : p.n0 + k;
@@ -495,23 +534,14 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
     const float2 nA = __ffma2_rn(lrA, R2, udA);
     const float2 nB = __ffma2_rn(lrB, R2, udB);
     {
-      const float4 co = coefrow<MODE>(p, x, coef4, r);
+      const float4 co = coefrow<MODE, CS>(p, x, coef4, r);
       const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), Q2, nA);
       const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), Q2, nB);
       if (MODE == MODE_REC) {
-        // Q = dy^2 lap (the adjoint's flush scale carries the 1 / dy^2), whole
-        // owned rows in one 16-byte store; the per-column form only in the rare
-        // warps holding a lane that owns part of its columns
-        const float l0 = lA.x, l1 = lA.y, l2 = lB.x, l3 = lB.y;
-        float* dst = segrow + (long long)r * p.pitch;
-        if ((x.rfull >> r) & 1u) {
-          *reinterpret_cast<float4*>(dst) = make_float4(l0, l1, l2, l3);
-        } else if ((x.rpart >> r) & 1u) {
-          if (x.own_cols & 1u) dst[0] = l0;
-          if (x.own_cols & 2u) dst[1] = l1;
-          if (x.own_cols & 4u) dst[2] = l2;
-          if (x.own_cols & 8u) dst[3] = l3;
-        }
+        // Q = dy^2 lap (the adjoint's flush scale carries the 1 / dy^2): each
+        // owned row in one predicated 16-byte store
+        if ((x.rfull >> r) & 1u) *reinterpret_cast<float4*>(segrow) = make_float4(lA.x, lA.y, lB.x, lB.y);
+        segrow += p.pitch;
       }
       const float2 tA = __ffma2_rn(TWO2, make_float2(cur.x, cur.y), make_float2(-P[r][0], -P[r][1]));
       const float2 tB = __ffma2_rn(TWO2, make_float2(cur.z, cur.w), make_float2(-P[r][2], -P[r][3]));
@@ -580,38 +610,8 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
   if (MODE == MODE_ADJ && x.own_rows) {  // warp-uniform: the tensor-memory ops are warp-wide
     if (n >= 1) {
-      // lap(u^{n-1}) of this thread's owned cells was streamed into shared
-      // memory (cp.async) during the previous step
-      cp_async_wait_all();
-      __syncwarp();  // the tensor-memory instructions need the whole warp converged
-      tm_wait_st();
-      const float4* l4 = reinterpret_cast<const float4*>(x.s_lap) + (x.w * KY) * 32 + x.lane;
-#pragma unroll
-      for (int r = 0; r < KY; r += 2) {
-        if ((x.own_rows >> r) & 3u) {
-          // rows r and r+1, all four columns: a cell this thread does not own
-          // sums whatever its Laplacian slot holds, and is never flushed
-          unsigned v[8];
-          tm_ld8(x.tm + 4 * r, v);
-          const float4 la = l4[r * 32];
-          const float4 lb = l4[(r + 1) * 32];
-          tm_wait_ld();
-          float2 g;
-          g = __ffma2_rn(make_float2(P[r][0], P[r][1]), make_float2(la.x, la.y),
-                         make_float2(__uint_as_float(v[0]), __uint_as_float(v[1])));
-          v[0] = __float_as_uint(g.x); v[1] = __float_as_uint(g.y);
-          g = __ffma2_rn(make_float2(P[r][2], P[r][3]), make_float2(la.z, la.w),
-                         make_float2(__uint_as_float(v[2]), __uint_as_float(v[3])));
-          v[2] = __float_as_uint(g.x); v[3] = __float_as_uint(g.y);
-          g = __ffma2_rn(make_float2(P[r + 1][0], P[r + 1][1]), make_float2(lb.x, lb.y),
-                         make_float2(__uint_as_float(v[4]), __uint_as_float(v[5])));
-          v[4] = __float_as_uint(g.x); v[5] = __float_as_uint(g.y);
-          g = __ffma2_rn(make_float2(P[r + 1][2], P[r + 1][3]), make_float2(lb.z, lb.w),
-                         make_float2(__uint_as_float(v[6]), __uint_as_float(v[7])));
-          v[6] = __float_as_uint(g.x); v[7] = __float_as_uint(g.y);
-          tm_st8(x.tm + 4 * r, v);
-        }
-      }
+      if (x.own_rows == (1u << KY) - 1u) image_band<KY, true>(x, P);
+      else image_band<KY, false>(x, P);
     }
     if (x.own_cols && k + 1 < p.nsteps && n - 1 >= 1) prefetch_lap<KY>(p, x, n - 1);
   }
@@ -640,7 +640,7 @@ __device__ __forceinline__ float4 pml_face_y(const float4& po, const float4& sxc
 // next band's first row and its published old psi_y, so one barrier per step
 // still suffices. Sources, receivers, the recompute's Laplacian and the imaging
 // are as in substep; where sigma = 0 the values are bit for bit the plain ones.
-template <int KY, int MODE>
+template <int KY, int MODE, bool CS>
 __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4], const TbParams& p,
                                             const Ctx& x, int k) {
   const int n = (MODE == MODE_ADJ) ? p.n0 - k : p.n0 + k;
@@ -708,18 +708,11 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
     const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), Q2, nA);
     const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), Q2, nB);
     if (MODE == MODE_REC) {
-      const float2 gA = lA, gB = lB;  // Q = dy^2 lap, as substep stores it
-      float* dst = segrow + (long long)r * p.pitch;
-      if ((x.rfull >> r) & 1u) {
-        *reinterpret_cast<float4*>(dst) = make_float4(gA.x, gA.y, gB.x, gB.y);
-      } else if ((x.rpart >> r) & 1u) {
-        if (x.own_cols & 1u) dst[0] = gA.x;
-        if (x.own_cols & 2u) dst[1] = gA.y;
-        if (x.own_cols & 4u) dst[2] = gB.x;
-        if (x.own_cols & 8u) dst[3] = gB.y;
-      }
+      // Q = dy^2 lap, as substep stores it
+      if ((x.rfull >> r) & 1u) *reinterpret_cast<float4*>(segrow) = make_float4(lA.x, lA.y, lB.x, lB.y);
+      segrow += p.pitch;
     }
-    const float4 co = coefrow<MODE>(p, x, coef4, r);
+    const float4 co = coefrow<MODE, CS>(p, x, coef4, r);
     float A, M;
     pml_factors(sxc.x, sy, p.hdt, p.dt2, A, M);
     P[r][0] = pml_leap(cur.x, P[r][0], co.x, A, M, lA.x, pml_div(pxl.x, pxl.y, pyb.x, pyt.x));
@@ -778,36 +771,7 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
     }
   }
   if (MODE == MODE_ADJ && x.own_rows) {
-    if (n >= 1) {
-      cp_async_wait_all();
-      __syncwarp();
-      tm_wait_st();
-      const float4* l4 = reinterpret_cast<const float4*>(x.s_lap) + (x.w * KY) * 32 + x.lane;
-#pragma unroll
-      for (int r = 0; r < KY; r += 2) {
-        if ((x.own_rows >> r) & 3u) {
-          unsigned v[8];
-          tm_ld8(x.tm + 4 * r, v);
-          const float4 la = l4[r * 32];
-          const float4 lb = l4[(r + 1) * 32];
-          tm_wait_ld();
-          float2 g;
-          g = __ffma2_rn(make_float2(P[r][0], P[r][1]), make_float2(la.x, la.y),
-                         make_float2(__uint_as_float(v[0]), __uint_as_float(v[1])));
-          v[0] = __float_as_uint(g.x); v[1] = __float_as_uint(g.y);
-          g = __ffma2_rn(make_float2(P[r][2], P[r][3]), make_float2(la.z, la.w),
-                         make_float2(__uint_as_float(v[2]), __uint_as_float(v[3])));
-          v[2] = __float_as_uint(g.x); v[3] = __float_as_uint(g.y);
-          g = __ffma2_rn(make_float2(P[r + 1][0], P[r + 1][1]), make_float2(lb.x, lb.y),
-                         make_float2(__uint_as_float(v[4]), __uint_as_float(v[5])));
-          v[4] = __float_as_uint(g.x); v[5] = __float_as_uint(g.y);
-          g = __ffma2_rn(make_float2(P[r + 1][2], P[r + 1][3]), make_float2(lb.z, lb.w),
-                         make_float2(__uint_as_float(v[6]), __uint_as_float(v[7])));
-          v[6] = __float_as_uint(g.x); v[7] = __float_as_uint(g.y);
-          tm_st8(x.tm + 4 * r, v);
-        }
-      }
-    }
+    if (n >= 1) image_band<KY, false>(x, P);
     if (x.own_cols && k + 1 < p.nsteps && n - 1 >= 1) prefetch_lap<KY>(p, x, n - 1);
   }
 
@@ -890,17 +854,17 @@ __device__ __forceinline__ void prefetch_state(const TbParams& p, const Ctx& x, 
 
 // The T steps of one item; the item setup has published the band's first and
 // last rows and met the whole CTA.
-template <int KY, int MODE, int EK>
+template <int KY, int MODE, int EK, bool CS>
 __device__ __forceinline__ void run_item(const TbParams& p, const Ctx& x, float (&P)[KY][4], float (&C)[KY][4]) {
   if (MODE == MODE_ADJ && x.own_rows && x.own_cols && p.n0 >= 1) prefetch_lap<KY>(p, x, p.n0);
 
   for (int k = 0; k < p.nsteps; k += 2) {
     if constexpr (EK == EK_PML) {
-      substep_pml<KY, MODE>(P, C, p, x, k);
-      if (k + 1 < p.nsteps) substep_pml<KY, MODE>(C, P, p, x, k + 1);
+      substep_pml<KY, MODE, CS>(P, C, p, x, k);
+      if (k + 1 < p.nsteps) substep_pml<KY, MODE, CS>(C, P, p, x, k + 1);
     } else {
-      substep<KY, MODE, EK>(P, C, p, x, k);
-      if (k + 1 < p.nsteps) substep<KY, MODE, EK>(C, P, p, x, k + 1);
+      substep<KY, MODE, EK, CS>(P, C, p, x, k);
+      if (k + 1 < p.nsteps) substep<KY, MODE, EK, CS>(C, P, p, x, k + 1);
     }
   }
   // the item's end reads every warp's staged taps; with CTA-wide step barriers
@@ -933,9 +897,26 @@ __device__ __forceinline__ void bind_ctx(const TbParams& p, Ctx& x, unsigned cha
   x.s_src = reinterpret_cast<float*>(smem + L.src);
 }
 
+// The loop variant of one warp for one item; CS: the coefficient tile is in shared
+// memory (every mode but an adjoint without room for it), a compile-time choice (a
+// kernel of its own) so that the step loop has no per-row branch on it.
+template <int KY, int MODE, bool PML, bool CS>
+__device__ __forceinline__ void dispatch_item(const TbParams& p, const Ctx& x, float (&P)[KY][4], float (&C)[KY][4],
+                                              int ek) {
+  if constexpr (PML) {
+    if (ek == EK_PML) {
+      run_item<KY, MODE, EK_PML, CS>(p, x, P, C);
+      return;
+    }
+  }
+  if (ek == EK_NONE) run_item<KY, MODE, EK_NONE, CS>(p, x, P, C);
+  else if (ek == EK_EDGE) run_item<KY, MODE, EK_EDGE, CS>(p, x, P, C);
+  else if (ek == EK_ALL) run_item<KY, MODE, EK_ALL, CS>(p, x, P, C);
+}
+
 // One (tile, shot) item: load, T steps, store, traces / gradient flush; `next` is
 // the CTA's next item of the same launch (or -1), whose state is prefetched.
-template <int KY, int MODE, bool PML>
+template <int KY, int MODE, bool PML, bool CS>
 __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char* smem, int item, int next) {
   const int nw = p.nwarps;
   const int nthr = nw * 32;
@@ -969,8 +950,16 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
       const int xx = x.xb + c;
       if (xx >= t.ox0 && xx < t.ox1) x.own_cols |= 1u << c;
     }
-    x.rfull = (x.own_cols == 0xFu) ? x.own_rows : 0u;
-    x.rpart = (x.own_cols != 0xFu && x.own_cols) ? x.own_rows : 0u;
+    // (padding columns beyond nx count as owned: no other tile writes them, and
+    // the adjoint never reads them back into the gradient; gradient plans place
+    // every other ownership boundary between lanes)
+    {
+      unsigned ext = x.own_cols;
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (x.xb + c >= p.nx) ext |= 1u << c;
+      x.rfull = (x.own_cols && ext == 0xFu) ? x.own_rows : 0u;
+    }
     float P[KY][4], C[KY][4];
     load_state<KY>(p, x, P, C);
     if (next >= 0) prefetch_state<KY>(p, x, next);
@@ -1169,17 +1158,8 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
     const bool cols = t.flags & (TF_LEFT | TF_RIGHT);
     const bool fast = (!row_b || x.y0 == 0) && (!row_t || x.y0 + KY == p.ny) && !(row_b && row_t) &&
                       (!(t.flags & TF_RIGHT) || ((p.nx - 1 - t.rx0) & 3) != 0);
-    if constexpr (PML) {
-      if (pml_warp) run_item<KY, MODE, EK_PML>(p, x, P, C);
-    }
-    if (pml_warp) {
-    } else if (!row_b && !row_t && !cols) {
-      run_item<KY, MODE, EK_NONE>(p, x, P, C);
-    } else if (fast) {
-      run_item<KY, MODE, EK_EDGE>(p, x, P, C);
-    } else {
-      run_item<KY, MODE, EK_ALL>(p, x, P, C);
-    }
+    const int ek = pml_warp ? EK_PML : (!row_b && !row_t && !cols) ? EK_NONE : fast ? EK_EDGE : EK_ALL;
+    dispatch_item<KY, MODE, PML, CS>(p, x, P, C, ek);
 
     if (PML && x.slot && x.own_rows && x.own_cols) {
       // the face fields of the owned cells (cells without a slot hold zero there,
@@ -1267,7 +1247,7 @@ __device__ __forceinline__ void tm_end(const Ctx& x, unsigned base) {
   if (x.w == 0) tm_dealloc(base);
 }
 
-template <int KY, int MODE, int MAXT, bool PML>
+template <int KY, int MODE, int MAXT, bool PML, bool CS>
 __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ unsigned tm_slot;
@@ -1282,14 +1262,16 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   // grid stride: at any moment the CTAs hold a mix of edge, interior and
   // receiver-heavy tiles, which balances better than contiguous runs per CTA.
   for (int item = blockIdx.x; item < nitems; item += gridDim.x)
-    run_one<KY, MODE, PML>(p, x, smem, item, item + (int)gridDim.x < nitems ? item + (int)gridDim.x : -1);
+    run_one<KY, MODE, PML, CS>(p, x, smem, item, item + (int)gridDim.x < nitems ? item + (int)gridDim.x : -1);
   tm_end<MODE>(x, tm_base);
 }
 
 // Several plans (grids) of one launch shape in one launch: the items of plan i
 // are [item_off[i], item_off[i+1]); a CTA copies the parameters of the plan of
-// its current item into shared memory when the plan changes.
-template <int KY, int MODE, int MAXT>
+// its current item into shared memory when the plan changes. CS: every plan of the
+// group keeps its coefficient tile in shared memory (reading it through L1 serves
+// any plan).
+template <int KY, int MODE, int MAXT, bool CS>
 __global__ void __launch_bounds__(MAXT, 1) tb_group_kernel(const TbGroup g) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(16) TbParams sp;
@@ -1312,16 +1294,16 @@ __global__ void __launch_bounds__(MAXT, 1) tb_group_kernel(const TbGroup g) {
       bind_ctx<KY, MODE>(sp, x, smem);
       cur = pi;
     }
-    run_one<KY, MODE, false>(sp, x, smem, item - __ldg(g.item_off + pi), -1);
+    run_one<KY, MODE, false, CS>(sp, x, smem, item - __ldg(g.item_off + pi), -1);
   }
   tm_end<MODE>(x, tm_base);
 }
 
-template <int KY, int MODE, int MAXT, bool PML>
+template <int KY, int MODE, int MAXT, bool PML, bool CS>
 cudaError_t configure_one(size_t smem) {
   static size_t configured_smem = 0;  // per device it is the same binary; raise only
   if (smem > configured_smem) {
-    cudaError_t e = cudaFuncSetAttribute(tb_kernel<KY, MODE, MAXT, PML>,
+    cudaError_t e = cudaFuncSetAttribute(tb_kernel<KY, MODE, MAXT, PML, CS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     configured_smem = smem;
@@ -1329,50 +1311,99 @@ cudaError_t configure_one(size_t smem) {
   return cudaSuccess;
 }
 
-template <int KY, int MODE, int MAXT, bool PML>
+template <int KY, int MODE, int MAXT, bool PML, bool CS>
 cudaError_t launch_one(const TbParams& p, int grid, size_t smem, cudaStream_t st) {
-  cudaError_t e = configure_one<KY, MODE, MAXT, PML>(smem);
+  cudaError_t e = configure_one<KY, MODE, MAXT, PML, CS>(smem);
   if (e != cudaSuccess) return e;
-  tb_kernel<KY, MODE, MAXT, PML><<<grid, p.nwarps * 32, smem, st>>>(p);
+  tb_kernel<KY, MODE, MAXT, PML, CS><<<grid, p.nwarps * 32, smem, st>>>(p);
   return cudaGetLastError();
 }
 
-template <int KY, int MAXT, bool PML>
-cudaError_t launch_mode(const TbParams& p, int mode, int grid, size_t smem, cudaStream_t st) {
-  if (mode == MODE_FWD) return launch_one<KY, MODE_FWD, MAXT, PML>(p, grid, smem, st);
-  if (mode == MODE_REC) return launch_one<KY, MODE_REC, MAXT, PML>(p, grid, smem, st);
-  return launch_one<KY, MODE_ADJ, MAXT, PML>(p, grid, smem, st);
+// One mode at one shape; the adjoint has a kernel with its coefficient tile in
+// shared memory and one that reads it through L1.
+template <int KY, int MODE, int MAXT, bool PML>
+cudaError_t launch_fixed(const TbParams& p, int grid, size_t smem, cudaStream_t st) {
+  if constexpr (MODE == MODE_ADJ) {
+    if (!p.adj_coef) return launch_one<KY, MODE, MAXT, PML, false>(p, grid, smem, st);
+  }
+  return launch_one<KY, MODE, MAXT, PML, true>(p, grid, smem, st);
 }
 
-template <int KY, int MAXT, bool PML>
-cudaError_t configure_mode(int mode, size_t smem) {
-  if (mode == MODE_FWD) return configure_one<KY, MODE_FWD, MAXT, PML>(smem);
-  if (mode == MODE_REC) return configure_one<KY, MODE_REC, MAXT, PML>(smem);
-  return configure_one<KY, MODE_ADJ, MAXT, PML>(smem);
+template <int KY, int MODE, int MAXT, bool PML>
+cudaError_t configure_fixed(size_t smem) {
+  cudaError_t e = configure_one<KY, MODE, MAXT, PML, true>(smem);
+  if constexpr (MODE == MODE_ADJ) {
+    if (e == cudaSuccess) e = configure_one<KY, MODE, MAXT, PML, false>(smem);
+  }
+  return e;
 }
 
 // The four launch shapes: KY = 8 rows per lane with at most 12 warps (168
 // registers per thread) or 16 warps (128 registers); KY = 4 with at most 16 warps
-// (128 registers) or 32 warps (64 registers).
-template <bool PML>
-cudaError_t launch_shape(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st) {
+// (128 registers) or 32 warps (64 registers). One mode per instantiation, so that
+// the modes compile in translation units of their own, in parallel.
+template <int MODE, bool PML>
+cudaError_t launch_shape(const TbParams& p, int ky, int grid, size_t smem, cudaStream_t st) {
   if (ky == 8) {
-    if (p.nwarps <= 12) return launch_mode<8, 384, PML>(p, mode, grid, smem, st);
-    return launch_mode<8, 512, PML>(p, mode, grid, smem, st);
+    if (p.nwarps <= 12) return launch_fixed<8, MODE, 384, PML>(p, grid, smem, st);
+    return launch_fixed<8, MODE, 512, PML>(p, grid, smem, st);
   }
-  if (p.nwarps <= 16) return launch_mode<4, 512, PML>(p, mode, grid, smem, st);
-  return launch_mode<4, 1024, PML>(p, mode, grid, smem, st);
+  if (p.nwarps <= 16) return launch_fixed<4, MODE, 512, PML>(p, grid, smem, st);
+  return launch_fixed<4, MODE, 1024, PML>(p, grid, smem, st);
 }
 
-template <bool PML>
-cudaError_t configure_shape(int ky, int mode, int nwarps, size_t smem) {
+template <int MODE, bool PML>
+cudaError_t configure_shape(int ky, int nwarps, size_t smem) {
   if (ky == 8) {
-    if (nwarps <= 12) return configure_mode<8, 384, PML>(mode, smem);
-    return configure_mode<8, 512, PML>(mode, smem);
+    if (nwarps <= 12) return configure_fixed<8, MODE, 384, PML>(smem);
+    return configure_fixed<8, MODE, 512, PML>(smem);
   }
-  if (nwarps <= 16) return configure_mode<4, 512, PML>(mode, smem);
-  return configure_mode<4, 1024, PML>(mode, smem);
+  if (nwarps <= 16) return configure_fixed<4, MODE, 512, PML>(smem);
+  return configure_fixed<4, MODE, 1024, PML>(smem);
+}
+
+template <int KY, int MODE, int MAXT, bool CS>
+cudaError_t group_one(const TbGroup& g, int nwarps, int grid, size_t smem, cudaStream_t st) {
+  static size_t configured_smem = 0;
+  if (smem > configured_smem) {
+    cudaError_t e = cudaFuncSetAttribute(tb_group_kernel<KY, MODE, MAXT, CS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured_smem = smem;
+  }
+  tb_group_kernel<KY, MODE, MAXT, CS><<<grid, nwarps * 32, smem, st>>>(g);
+  return cudaGetLastError();
+}
+
+template <int KY, int MODE, int MAXT>
+cudaError_t group_fixed(const TbGroup& g, int nwarps, bool adj_coef, int grid, size_t smem, cudaStream_t st) {
+  if constexpr (MODE == MODE_ADJ) {
+    if (!adj_coef) return group_one<KY, MODE, MAXT, false>(g, nwarps, grid, smem, st);
+  }
+  return group_one<KY, MODE, MAXT, true>(g, nwarps, grid, smem, st);
+}
+
+template <int MODE>
+cudaError_t group_shape(const TbGroup& g, int ky, int nwarps, bool adj_coef, int grid, size_t smem,
+                        cudaStream_t st) {
+  if (ky == 8) {
+    if (nwarps <= 12) return group_fixed<8, MODE, 384>(g, nwarps, adj_coef, grid, smem, st);
+    return group_fixed<8, MODE, 512>(g, nwarps, adj_coef, grid, smem, st);
+  }
+  if (nwarps <= 16) return group_fixed<4, MODE, 512>(g, nwarps, adj_coef, grid, smem, st);
+  return group_fixed<4, MODE, 1024>(g, nwarps, adj_coef, grid, smem, st);
 }
 
 }  // namespace
+
+// Entry points of the translation units (one per family and mode group).
+cudaError_t tb_launch_adj(const TbParams& p, int ky, int grid, size_t smem, cudaStream_t st);
+cudaError_t tb_configure_adj(int ky, int nwarps, size_t smem);
+cudaError_t tb_group_launch_adj(const TbGroup& g, int ky, int nwarps, bool adj_coef, int grid, size_t smem,
+                                cudaStream_t st);
+cudaError_t tb_launch_pml(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st);
+cudaError_t tb_configure_pml(int ky, int mode, int nwarps, size_t smem);
+cudaError_t tb_launch_pml_adj(const TbParams& p, int ky, int grid, size_t smem, cudaStream_t st);
+cudaError_t tb_configure_pml_adj(int ky, int nwarps, size_t smem);
+
 }  // namespace fdtd
