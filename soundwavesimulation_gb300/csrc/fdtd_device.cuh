@@ -207,6 +207,12 @@ struct TbParams {
   int nrow_max, nrxl_max, tmax;  // nrow_max: staged tap rows of the largest tile
   int adj_coef;          // adjoint: 1 = coefficient tile in shared memory, 0 = read through L1
   int pair_sync;         // 1: neighbouring warps meet on named barriers after a step, 0: the CTA
+  // item scheduling: CTA b first runs the static run [b * static_items, (b + 1) *
+  // static_items) (consecutive shots of mostly one tile, whose shot-independent
+  // tables it keeps), then takes single items from the counter sched (zeroed before
+  // the launch) after the static runs; sched == nullptr: a grid stride
+  int* sched;
+  int static_items;
   // sources
   const SrcNode* src;    // (nshots, nsrc_max) merged injection nodes
   int nsrc_max;

@@ -133,6 +133,8 @@ struct fdtd_plan {
   size_t o_apsi[2][2] = {{0, 0}, {0, 0}};
   size_t o_ckpsi = 0;
   size_t o_ckpt = 0, ckpt_elem_bytes = 4, o_scales = 0, o_seg = 0, o_graw = 0;
+  size_t o_sched = 0;  // one item counter per temporally blocked launch of a pass
+  int n_sched = 0;
   size_t total = 0;
   size_t smem[3] = {0, 0, 0};
   // binding
@@ -261,7 +263,12 @@ int grid_size(const fdtd_plan* p) {
 float* fptr(fdtd_plan* p, size_t off) { return reinterpret_cast<float*>(p->ws + off); }
 
 int32_t launch(fdtd_plan* p, TbParams& q, int mode, cudaStream_t st) {
-  cudaError_t e = tb_launch(q, p->ky, mode, grid_size(p), p->smem[mode], st);
+  // 85 % of the items in static runs of consecutive shots, the rest dealt out one
+  // by one to whichever CTA is free (the tail balances; the runs reuse tiles)
+  const int grid = grid_size(p);
+  const int items = (int)p->tiles.size() * p->prob.n_shots;
+  q.static_items = (q.sched && mode == MODE_FWD) ? (int)(0.85 * items / grid) : 0;
+  cudaError_t e = tb_launch(q, p->ky, mode, grid, p->smem[mode], st);
   if (e != cudaSuccess) return cuda_fail(e, "temporally blocked kernel launch");
   return FDTD_OK;
 }
@@ -893,6 +900,15 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   const size_t fb = p->field_elems * sizeof(float);
   size_t off = 0;
   p->o_tiles = off; off = align_up(off + p->tiles.size() * sizeof(TbTile));
+  {
+    // launches per pass: the forward ceil(nt / T); the adjoint pass recomputes and
+    // images every segment (ceil(C / T) launches each way per segment)
+    const int nt = problem->n_steps, T = p->tmax;
+    const int fwd = (nt + T - 1) / T;
+    const int seg = (p->ckpt_every + T - 1) / T;
+    p->n_sched = std::max(fwd, p->for_gradient ? 2 * seg * p->nseg : 0) + 1;
+    p->o_sched = off; off = align_up(off + (size_t)p->n_sched * sizeof(int));
+  }
   p->o_taps = off; off = align_up(off + std::max<size_t>(1, p->taps.size()) * sizeof(TbTap));
   p->o_tmask = off; off = align_up(off + p->tmask.size() * sizeof(TbMask));
   p->o_rxl = off; off = align_up(off + std::max<size_t>(1, p->rxl.size()) * sizeof(int));
@@ -1092,6 +1108,7 @@ struct Sink {
   fdtd_plan* p;
   cudaStream_t st;
   std::vector<Op>* rec;
+  int nsched = 0;  // item counters used so far in this pass
   int32_t emit(const Op& op) {
     if (rec) {
       rec->push_back(op);
@@ -1108,8 +1125,15 @@ struct Sink {
     op.kind = Op::LAUNCH;
     op.mode = mode;
     op.q = q;
+    op.q.sched = nullptr;
+    if (!rec) {  // a launch of its own (grouped launches deal items with a grid stride)
+      if (nsched >= p->n_sched) return fail(FDTD_ERR_STATE, "item counters exhausted");
+      op.q.sched = reinterpret_cast<int*>(p->ws + p->o_sched) + nsched++;
+    }
     return emit(op);
   }
+  // the pass's item counters start at zero
+  int32_t reset_sched() { return memset(p->ws + p->o_sched, (size_t)p->n_sched * sizeof(int)); }
   int32_t memset(void* dst, size_t bytes) {
     Op op;
     op.kind = Op::MEMSET;
@@ -1159,7 +1183,8 @@ struct Sink {
 int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u_out,
                         int32_t save_checkpoints, Sink& k) {
   const size_t fb = p->field_elems * sizeof(float);
-  int32_t rc0 = k.memset(p->ws + p->o_state[0][0], fb);
+  int32_t rc0 = k.reset_sched();
+  if (!rc0) rc0 = k.memset(p->ws + p->o_state[0][0], fb);
   if (!rc0) rc0 = k.memset(p->ws + p->o_state[0][1], fb);
   if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_psi[0][0], fb);
   if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_psi[0][1], fb);
@@ -1237,7 +1262,8 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
 
 int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Sink& k) {
   const size_t fb = p->field_elems * sizeof(float);
-  int32_t rc0 = k.memset(p->ws + p->o_adj[0][0], fb);
+  int32_t rc0 = k.reset_sched();
+  if (!rc0) rc0 = k.memset(p->ws + p->o_adj[0][0], fb);
   if (!rc0) rc0 = k.memset(p->ws + p->o_adj[0][1], fb);
   if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_apsi[0][0], fb);
   if (!rc0 && p->pml) rc0 = k.memset(p->ws + p->o_apsi[0][1], fb);

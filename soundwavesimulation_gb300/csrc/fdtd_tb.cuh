@@ -59,6 +59,7 @@ constexpr int EK_PML = 3;
 
 struct Ctx {
   int tid, w, lane, nw, s;
+  int cur_tile;             // the tile whose shot-independent tables shared memory holds (-1: none)
   int rx0, ry0, flags;
   int y0, xb;               // global row of this thread's r = 0, column of c = 0
   unsigned own_rows, own_cols;
@@ -915,9 +916,13 @@ __device__ __forceinline__ void dispatch_item(const TbParams& p, const Ctx& x, f
 }
 
 // One (tile, shot) item: load, T steps, store, traces / gradient flush; `next` is
-// the CTA's next item of the same launch (or -1), whose state is prefetched.
+// the CTA's next item of the same launch (or -1), whose state is prefetched; with
+// dyn_next it is read from there after the item's first CTA barrier. The region's
+// coefficient tile, Mur table and PML tables are kept from the previous item when
+// it was the same tile (consecutive shots of a static run).
 template <int KY, int MODE, bool PML, bool CS>
-__device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char* smem, int item, int next) {
+__device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char* smem, int item, int next,
+                                        const int* dyn_next = nullptr) {
   const int nw = p.nwarps;
   const int nthr = nw * 32;
   const TbSmem L = tb_smem_layout(nw, KY, MODE, p.nrow_max, p.nrxl_max, p.tmax, p.adj_coef, p.nsrow_max,
@@ -929,6 +934,10 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
     const int ti = item / p.nshots;
     const int s = item - ti * p.nshots;
     const TbTile t = p.tiles[ti];
+    // (the forward only: the recompute and adjoint, at their register limit, deal
+    // their items with a grid stride, where consecutive items are other tiles)
+    const bool same_tile = MODE == MODE_FWD && ti == x.cur_tile;  // CTA-uniform
+    if (MODE == MODE_FWD) x.cur_tile = ti;
     x.s = s;
     x.rx0 = t.rx0;
     x.ry0 = t.ry0;
@@ -973,7 +982,7 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
     constexpr bool ASYNC_FILL = MODE == MODE_FWD;
 #pragma unroll
     for (int r = 0; r < KY; ++r) {
-      if (MODE != MODE_ADJ || p.adj_coef) {
+      if (!same_tile && (MODE != MODE_ADJ || p.adj_coef)) {
         float4* dst = reinterpret_cast<float4*>(x.s_coef) + (x.w * KY + r) * 32 + x.lane;
         if (ASYNC_FILL && ((x.rowvalid >> r) & 1u)) {
           cp_async16(dst, x.gcoef + (long long)r * p.pitch);
@@ -1001,18 +1010,20 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
       const int RYp = nw * KY + 1;
       float* pc = const_cast<float*>(x.s_pcol);
       float* pr = const_cast<float*>(x.s_prow);
-      for (int i = x.tid; i < PML_TABLES * RX; i += nthr) {
-        const int tbl = i / RX, gx = t.rx0 + i - tbl * RX;
-        pc[i] = (gx >= 0 && gx < p.nx) ? __ldg(p.pml + tbl * p.nx + gx) : 0.f;
-      }
-      for (int i = x.tid; i < PML_TABLES * RYp; i += nthr) {
-        const int tbl = i / RYp, gy = t.ry0 + i - tbl * RYp;
-        pr[i] = (gy >= 0 && gy < p.ny) ? __ldg(p.pml + PML_TABLES * p.nx + tbl * p.ny + gy) : 0.f;
+      if (!same_tile) {
+        for (int i = x.tid; i < PML_TABLES * RX; i += nthr) {
+          const int tbl = i / RX, gx = t.rx0 + i - tbl * RX;
+          pc[i] = (gx >= 0 && gx < p.nx) ? __ldg(p.pml + tbl * p.nx + gx) : 0.f;
+        }
+        for (int i = x.tid; i < PML_TABLES * RYp; i += nthr) {
+          const int tbl = i / RYp, gy = t.ry0 + i - tbl * RYp;
+          pr[i] = (gy >= 0 && gy < p.ny) ? __ldg(p.pml + PML_TABLES * p.nx + tbl * p.ny + gy) : 0.f;
+        }
       }
       for (int i = x.tid; i < 2 * nw * 32; i += nthr) x.s_pxch[i] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (x.tid == 0) *reinterpret_cast<int*>(smem + L.nslot) = 0;
     }
-    if (t.flags & TF_MUR) {
+    if ((t.flags & TF_MUR) && !same_tile) {
       // the tile's Mur table: left / right k per region row, bottom / top per
       // region column, corner kx / ky; the adjoint also copies the ratio set
       const int ry = nw * KY, len = 2 * ry + 2 * RX + 8, glen = 2 * p.ny + 2 * p.nx + 8;
@@ -1144,6 +1155,10 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
       cp_async_wait_all();
     }
     __syncthreads();
+    if (dyn_next) {
+      const int nx_item = *dyn_next;
+      if (nx_item < p.ntiles * p.nshots) prefetch_state<KY>(p, x, nx_item);
+    }
     x.mask = (unsigned)tmk.x;
     x.base = tmk.y;
     x.smask = s_smask[x.tid];
@@ -1256,13 +1271,54 @@ __global__ void __launch_bounds__(MAXT, 1) tb_kernel(const TbParams p) {
   x.w = x.tid >> 5;
   x.lane = x.tid & 31;
   bind_ctx<KY, MODE>(p, x, smem);
+  x.cur_tile = -1;
   const unsigned tm_base = tm_begin<KY, MODE>(x, &tm_slot);
   const int nitems = p.ntiles * p.nshots;
-  // Items are (tile, shot) pairs with shots varying fastest, dealt out with a
-  // grid stride: at any moment the CTAs hold a mix of edge, interior and
-  // receiver-heavy tiles, which balances better than contiguous runs per CTA.
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x)
-    run_one<KY, MODE, PML, CS>(p, x, smem, item, item + (int)gridDim.x < nitems ? item + (int)gridDim.x : -1);
+  // Items are (tile, shot) pairs with shots varying fastest, the costliest tiles
+  // first. Each CTA runs a static run of consecutive items (mostly shots of one
+  // tile, whose coefficient tile and Mur table it keeps), then takes single items
+  // from a counter until none is left, so that CTAs whose runs were cheap take
+  // more and the launch ends within about one item of its mean. The next dynamic
+  // item is fetched by thread 0 at the start of the current one and read by all
+  // threads after that item's barriers (double-buffered).
+  // (one call site of run_one: the item code is inlined once)
+  __shared__ int s_dyn[2];
+  constexpr bool DYN = MODE == MODE_FWD;  // see run_one
+  const int S = (DYN && p.sched) ? p.static_items : 0;
+  const int s0 = (int)blockIdx.x * S, s1 = min(s0 + S, nitems);
+  const int d0 = min((int)gridDim.x * S, nitems);  // first dynamically dealt item
+  int par = 0;
+  int item = (int)blockIdx.x;
+  if (DYN && p.sched) {
+    item = s0 < s1 ? s0 : -1;
+    if (item < 0) {
+      if (x.tid == 0) s_dyn[0] = d0 + atomicAdd(p.sched, 1);
+      __syncthreads();
+      item = s_dyn[0];
+      par = 1;
+    }
+  }
+  while (item < nitems) {
+    int next = -1;
+    const int* dyn = nullptr;
+    if (!DYN || !p.sched) {
+      next = item + (int)gridDim.x < nitems ? item + (int)gridDim.x : -1;
+    } else if (item + 1 < s1) {
+      next = item + 1;
+    } else {
+      if (x.tid == 0) s_dyn[par] = d0 + atomicAdd(p.sched, 1);
+      dyn = &s_dyn[par];
+    }
+    run_one<KY, MODE, PML, CS>(p, x, smem, item, next, dyn);
+    if (!DYN || !p.sched) {
+      item += (int)gridDim.x;
+    } else if (!dyn) {
+      ++item;
+    } else {
+      item = s_dyn[par];
+      par ^= 1;
+    }
+  }
   tm_end<MODE>(x, tm_base);
 }
 
@@ -1292,6 +1348,7 @@ __global__ void __launch_bounds__(MAXT, 1) tb_group_kernel(const TbGroup g) {
       for (int i = x.tid; i < (int)(sizeof(TbParams) / sizeof(int)); i += blockDim.x) dst[i] = __ldg(src + i);
       __syncthreads();
       bind_ctx<KY, MODE>(sp, x, smem);
+      x.cur_tile = -1;
       cur = pi;
     }
     run_one<KY, MODE, false, CS>(sp, x, smem, item - __ldg(g.item_off + pi), -1);
