@@ -25,6 +25,9 @@ int32_t validate_plain_problem(const fdtd_problem& prob);
 
 // Temporally blocked kernel (fdtd_tb.cu).
 cudaError_t tb_launch(const TbParams& p, int ky, int mode, int grid, size_t smem, cudaStream_t st);
+// Shared memory the temporally blocked kernels may declare statically (reserved out
+// of the 227 KB per CTA when a plan sizes its dynamic shared memory).
+constexpr size_t TB_STATIC_SMEM = 64;
 // Sets the dynamic shared-memory attribute of the kernel a launch would use (the
 // PML family for pml).
 cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem, bool pml);

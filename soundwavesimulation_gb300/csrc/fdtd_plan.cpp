@@ -32,7 +32,9 @@ int32_t cuda_fail(cudaError_t e, const char* what) {
 namespace {
 
 constexpr size_t ALIGN = 256;
-constexpr size_t SMEM_LIMIT = 232448;  // 227 KB opt-in shared memory per CTA
+// 227 KB opt-in shared memory per CTA, less what the kernels declare statically
+// (the tensor-memory slot and the dynamic item buffers, 16 bytes; 64 reserved)
+constexpr size_t SMEM_LIMIT = 232448 - TB_STATIC_SMEM;
 
 size_t align_up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
 
@@ -264,10 +266,12 @@ float* fptr(fdtd_plan* p, size_t off) { return reinterpret_cast<float*>(p->ws + 
 
 int32_t launch(fdtd_plan* p, TbParams& q, int mode, cudaStream_t st) {
   // 85 % of the items in static runs of consecutive shots, the rest dealt out one
-  // by one to whichever CTA is free (the tail balances; the runs reuse tiles)
+  // by one to whichever CTA is free (the tail balances; the runs reuse tiles). A
+  // PML grid's layer tiles cost several times an interior tile, more than the
+  // dealt-out rest could balance: there every item is dealt out, costliest first.
   const int grid = grid_size(p);
   const int items = (int)p->tiles.size() * p->prob.n_shots;
-  q.static_items = (q.sched && mode == MODE_FWD) ? (int)(0.85 * items / grid) : 0;
+  q.static_items = (q.sched && mode == MODE_FWD && !p->pml) ? (int)(0.85 * items / grid) : 0;
   cudaError_t e = tb_launch(q, p->ky, mode, grid, p->smem[mode], st);
   if (e != cudaSuccess) return cuda_fail(e, "temporally blocked kernel launch");
   return FDTD_OK;
@@ -1498,7 +1502,7 @@ int32_t group_run(fdtd_plan* const* plans, int n, void* workspace, size_t bytes,
       items += plans[mb.first]->prob.n_shots * (int)plans[mb.first]->tiles.size();
       adj_coef = adj_coef && plans[mb.first]->adj_coef;
     }
-    if (smem + tb_group_static_smem() > SMEM_LIMIT) return fail(FDTD_ERR_UNSUPPORTED, "group: shared memory need exceeds 227 KB");
+    if (smem + tb_group_static_smem() > 232448) return fail(FDTD_ERR_UNSUPPORTED, "group: shared memory need exceeds 227 KB");
     TbGroup g;
     g.params = dparams + pk;
     g.item_off = doff + ok;

@@ -24,7 +24,7 @@ cudaError_t tb_group_launch(const TbGroup& g, int ky, int nwarps, int mode, bool
 size_t tb_group_static_smem() { return sizeof(TbParams) + 16; }
 
 cudaError_t tb_configure(int ky, int mode, int nwarps, size_t smem, bool pml) {
-  if (smem > 232448) return cudaSuccess;  // a mode this plan never launches
+  if (smem + TB_STATIC_SMEM > 232448) return cudaSuccess;  // a mode this plan never launches
   if (pml) return tb_configure_pml(ky, mode, nwarps, smem);
   if (mode == MODE_FWD) return configure_shape<MODE_FWD, false>(ky, nwarps, smem);
   if (mode == MODE_REC) return configure_shape<MODE_REC, false>(ky, nwarps, smem);
