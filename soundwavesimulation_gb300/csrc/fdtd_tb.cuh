@@ -611,8 +611,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
   if (MODE == MODE_ADJ && x.own_rows) {  // warp-uniform: the tensor-memory ops are warp-wide
     if (n >= 1) {
-      if (x.own_rows == (1u << KY) - 1u) image_band<KY, true>(x, P);
-      else image_band<KY, false>(x, P);
+      image_band<KY, false>(x, P);  // (a separate full-band copy made the adjoint spill)
     }
     if (x.own_cols && k + 1 < p.nsteps && n - 1 >= 1) prefetch_lap<KY>(p, x, n - 1);
   }
