@@ -213,40 +213,55 @@ __device__ __forceinline__ double widen(float f) {
   return __longlong_as_double((long long)b);
 }
 
+// One row pair of the imaging: v (the pair's gradient values from tensor memory) +=
+// F rows r, r+1 times their Laplacian rows la, lb, all four columns.
+template <int KY>
+__device__ __forceinline__ void image_pair(const float (&F)[KY][4], int r, const float4& la, const float4& lb,
+                                           unsigned (&v)[8]) {
+  float2 g;
+  g = __ffma2_rn(make_float2(F[r][0], F[r][1]), make_float2(la.x, la.y),
+                 make_float2(__uint_as_float(v[0]), __uint_as_float(v[1])));
+  v[0] = __float_as_uint(g.x); v[1] = __float_as_uint(g.y);
+  g = __ffma2_rn(make_float2(F[r][2], F[r][3]), make_float2(la.z, la.w),
+                 make_float2(__uint_as_float(v[2]), __uint_as_float(v[3])));
+  v[2] = __float_as_uint(g.x); v[3] = __float_as_uint(g.y);
+  g = __ffma2_rn(make_float2(F[r + 1][0], F[r + 1][1]), make_float2(lb.x, lb.y),
+                 make_float2(__uint_as_float(v[4]), __uint_as_float(v[5])));
+  v[4] = __float_as_uint(g.x); v[5] = __float_as_uint(g.y);
+  g = __ffma2_rn(make_float2(F[r + 1][2], F[r + 1][3]), make_float2(lb.z, lb.w),
+                 make_float2(__uint_as_float(v[6]), __uint_as_float(v[7])));
+  v[6] = __float_as_uint(g.x); v[7] = __float_as_uint(g.y);
+}
+
 // Imaging of this thread's band: the gradient tile in tensor memory += F times the
-// Laplacian tile that the previous step streamed into shared memory (cp.async), one
-// load-wait-store round trip per row pair, all four columns of a row (a cell this
-// thread does not own sums whatever its slot holds, and is never flushed). FULL: the
-// warp owns every row of its band (no per-pair test). Warp-uniform: the caller
-// checks own_rows.
-template <int KY, bool FULL>
+// Laplacian tile that the previous step streamed into shared memory (cp.async).
+// Row pairs are pipelined: the next pair's tensor-memory load is issued before the
+// current pair's arithmetic and store, so one load is always in flight. Every pair
+// is imaged, owned or not (a cell this thread does not own sums whatever its slot
+// holds, and is never flushed). Warp-uniform: the caller checks own_rows.
+template <int KY>
 __device__ __forceinline__ void image_band(const Ctx& x, const float (&F)[KY][4]) {
   cp_async_wait_all();
   __syncwarp();  // the tensor-memory instructions need the whole warp converged
   tm_wait_st();
   const float4* l4 = reinterpret_cast<const float4*>(x.s_lap) + (x.w * KY) * 32 + x.lane;
+  unsigned va[8], vb[8];  // gradient values of the even / odd row pairs
+  tm_ld8(x.tm, va);
 #pragma unroll
   for (int r = 0; r < KY; r += 2) {
-    if (FULL || ((x.own_rows >> r) & 3u)) {
-      unsigned v[8];
-      tm_ld8(x.tm + 4 * r, v);
-      const float4 la = l4[r * 32];
-      const float4 lb = l4[(r + 1) * 32];
-      tm_wait_ld();
-      float2 g;
-      g = __ffma2_rn(make_float2(F[r][0], F[r][1]), make_float2(la.x, la.y),
-                     make_float2(__uint_as_float(v[0]), __uint_as_float(v[1])));
-      v[0] = __float_as_uint(g.x); v[1] = __float_as_uint(g.y);
-      g = __ffma2_rn(make_float2(F[r][2], F[r][3]), make_float2(la.z, la.w),
-                     make_float2(__uint_as_float(v[2]), __uint_as_float(v[3])));
-      v[2] = __float_as_uint(g.x); v[3] = __float_as_uint(g.y);
-      g = __ffma2_rn(make_float2(F[r + 1][0], F[r + 1][1]), make_float2(lb.x, lb.y),
-                     make_float2(__uint_as_float(v[4]), __uint_as_float(v[5])));
-      v[4] = __float_as_uint(g.x); v[5] = __float_as_uint(g.y);
-      g = __ffma2_rn(make_float2(F[r + 1][2], F[r + 1][3]), make_float2(lb.z, lb.w),
-                     make_float2(__uint_as_float(v[6]), __uint_as_float(v[7])));
-      v[6] = __float_as_uint(g.x); v[7] = __float_as_uint(g.y);
-      tm_st8(x.tm + 4 * r, v);
+    const float4 la = l4[r * 32];
+    const float4 lb = l4[(r + 1) * 32];
+    tm_wait_ld();
+    // (the two buffers are named in separate branches, never selected by an
+    // expression, so that they stay in registers)
+    if ((r >> 1) & 1) {
+      if (r + 2 < KY) tm_ld8(x.tm + 4 * (r + 2), va);
+      image_pair<KY>(F, r, la, lb, vb);
+      tm_st8(x.tm + 4 * r, vb);
+    } else {
+      if (r + 2 < KY) tm_ld8(x.tm + 4 * (r + 2), vb);
+      image_pair<KY>(F, r, la, lb, va);
+      tm_st8(x.tm + 4 * r, va);
     }
   }
 }
@@ -611,7 +626,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   }
   if (MODE == MODE_ADJ && x.own_rows) {  // warp-uniform: the tensor-memory ops are warp-wide
     if (n >= 1) {
-      image_band<KY, false>(x, P);  // (a separate full-band copy made the adjoint spill)
+      image_band<KY>(x, P);
     }
     if (x.own_cols && k + 1 < p.nsteps && n - 1 >= 1) prefetch_lap<KY>(p, x, n - 1);
   }
@@ -771,7 +786,7 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
     }
   }
   if (MODE == MODE_ADJ && x.own_rows) {
-    if (n >= 1) image_band<KY, false>(x, P);
+    if (n >= 1) image_band<KY>(x, P);
     if (x.own_cols && k + 1 < p.nsteps && n - 1 >= 1) prefetch_lap<KY>(p, x, n - 1);
   }
 
