@@ -269,7 +269,10 @@ int32_t fdtd_plan_tuning(const fdtd_plan* plan, fdtd_tuning* tuning);
 /* Binds a caller-owned device workspace (256-byte aligned) and uploads the
    tables into it; synchronises `stream` once. */
 int32_t fdtd_plan_bind(fdtd_plan* plan, void* workspace, size_t bytes, void* stream);
-/* Updates the medium and source waveform pointers of a bound plan (same shapes). */
+/* Updates the medium and source waveform pointers of a bound plan (same shapes);
+   checkpoints become stale. The plan's captured CUDA graphs read the medium
+   through these pointers and are kept while the pointers stay the same (values
+   updated in place); a changed pointer makes the next pass capture again. */
 int32_t fdtd_plan_set_medium(fdtd_plan* plan, const float* coef, const float* mur,
                              const float* waveforms);
 

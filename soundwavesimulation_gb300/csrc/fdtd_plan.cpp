@@ -1021,11 +1021,17 @@ int32_t fdtd_plan_bind(fdtd_plan* p, void* workspace, size_t bytes, void* stream
 int32_t fdtd_plan_set_medium(fdtd_plan* p, const float* coef, const float* mur,
                              const float* waveforms) {
   if (!p) return fail(FDTD_ERR_INVALID, "null plan");
+  // The captured graphs read the medium through these pointers at run time: they
+  // stay valid while the pointers do (an in-place update of the values), and are
+  // captured again only when a pointer changes. Checkpoints of the old medium are
+  // stale either way.
+  const bool moved = (coef && coef != p->prob.grid.coef) || (mur && mur != p->prob.grid.mur) ||
+                     (waveforms && waveforms != p->prob.src.waveforms);
   if (coef) p->prob.grid.coef = coef;
   if (mur) p->prob.grid.mur = mur;
   if (waveforms) p->prob.src.waveforms = waveforms;
   p->have_ckpt = false;
-  p->drop_graphs();
+  if (moved) p->drop_graphs();
   return FDTD_OK;
 }
 

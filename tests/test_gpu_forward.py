@@ -291,6 +291,44 @@ def test_graph_replay_matches_eager_launches(tb):
     assert rel(out[0][1].cpu().numpy(), out[1][1].cpu().numpy()) < 1e-12
 
 
+def test_graph_kept_across_in_place_medium_updates(tb):
+    """A plan keeps its captured graph while the medium changes in place (same
+    buffers) and sees the new values: traces and gradient equal a fresh plan's on
+    the new medium, with the same output buffers (the graph replayed)."""
+    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan, residual_misfit
+    ny, nx, S, nt = 140, 121, 2, 47
+    p = _random_problem(ny, nx, S, 20, nt, seed=5)
+    waves = torch.as_tensor(p["waves"], dtype=torch.float32, device="cuda")
+    src = (p["srow"], p["scol"], p["sw"], p["wave"])
+    rx = (p["row0"], p["col0"], p["w"])
+    tun = {"steps_per_launch": 6}
+    medium = DeviceMedium(p["c"], p["dx"], p["dy"], p["dt"], "cuda")
+    plan = FusedPlan(medium, rx, src, waves, nt, tuning=tun, for_gradient=True)
+    tr = torch.empty((S, len(p["row0"]), nt), dtype=torch.float32, device="cuda")
+    res = torch.empty_like(tr)
+    zero = torch.zeros_like(tr)
+    g = torch.zeros((ny, medium.pitch), dtype=torch.float64, device="cuda")
+
+    def gradient():  # the same buffers every time: both graphs are replayed
+        plan.forward(tr, save_checkpoints=True)
+        residual_misfit(tr, zero, None, residual=res)
+        g.zero_()
+        plan.adjoint(res, g)
+
+    gradient()
+    c2 = p["c"] * 1.03
+    medium.set_c(c2)                       # in place: same coefficient buffers
+    gradient()
+    fresh_medium = DeviceMedium(c2, p["dx"], p["dy"], p["dt"], "cuda")
+    fresh = FusedPlan(fresh_medium, rx, src, waves, nt, tuning=tun, for_gradient=True)
+    tr2 = fresh.forward(save_checkpoints=True)
+    res2, _ = residual_misfit(tr2.clone(), torch.zeros_like(tr2), None)
+    g2 = torch.zeros_like(g)
+    fresh.adjoint(res2, g2)
+    assert torch.equal(tr, tr2)
+    assert rel(g.cpu().numpy(), g2.cpu().numpy()) < 1e-12
+
+
 @pytest.mark.parametrize("shape", [{"rows_per_lane": 8, "warps": 16}, {"rows_per_lane": 4, "warps": 32}])
 def test_plan_group_matches_separate_plans(tb, shape):
     """Three grids of different sizes, step counts and temporal-block depths in shared
