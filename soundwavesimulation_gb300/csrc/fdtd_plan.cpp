@@ -151,14 +151,24 @@ struct fdtd_plan {
     cudaGraphExec_t exec = nullptr;
     const void* key[4] = {nullptr, nullptr, nullptr, nullptr};
     int flag = 0;
+    unsigned long long used = 0;  // last replay (least recently used is replaced)
   };
-  Graph g_fwd, g_adj;
+  // A few captured passes per kind, keyed by their output pointers: a caller that
+  // alternates output buffers (a new traces tensor per call while the previous one
+  // is still alive) replays instead of capturing every call.
+  static constexpr int kGraphs = 4;
+  struct GraphSet {
+    Graph slot[kGraphs];
+  };
+  GraphSet g_fwd, g_adj;
+  unsigned long long graph_tick = 0;
   cudaStream_t capture_stream = nullptr;
   void drop_graphs() {
-    for (Graph* g : {&g_fwd, &g_adj}) {
-      if (g->exec) cudaGraphExecDestroy(g->exec);
-      *g = Graph();
-    }
+    for (GraphSet* gs : {&g_fwd, &g_adj})
+      for (Graph& g : gs->slot) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = Graph();
+      }
   }
   ~fdtd_plan() {
     drop_graphs();
@@ -1041,14 +1051,27 @@ namespace {
 
 // Runs `enqueue` on `st`, or replays it as a CUDA graph captured once per key.
 template <typename F>
-int32_t run_graphed(fdtd_plan* p, fdtd_plan::Graph& g, const void* const (&key)[4], int flag,
+int32_t run_graphed(fdtd_plan* p, fdtd_plan::GraphSet& gs, const void* const (&key)[4], int flag,
                     cudaStream_t st, F enqueue) {
   if (p->tun.eager) return enqueue(st);
-  bool hit = g.exec != nullptr && g.flag == flag;
-  for (int i = 0; i < 4 && hit; ++i) hit = g.key[i] == key[i];
+  fdtd_plan::Graph* found = nullptr;
+  fdtd_plan::Graph* victim = &gs.slot[0];
+  for (fdtd_plan::Graph& c : gs.slot) {
+    bool hit = c.exec != nullptr && c.flag == flag;
+    for (int i = 0; i < 4 && hit; ++i) hit = c.key[i] == key[i];
+    if (hit) {
+      found = &c;
+      break;
+    }
+    if (!c.exec || (victim->exec && c.used < victim->used)) victim = &c;
+  }
+  const bool hit = found != nullptr;
+  fdtd_plan::Graph& g = hit ? *found : *victim;
+  g.used = ++p->graph_tick;
   if (!hit) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = fdtd_plan::Graph();
+    g.used = p->graph_tick;
     cudaError_t e = cudaSuccess;
     if (!p->capture_stream) e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_fail(e, "capture stream");
