@@ -59,10 +59,10 @@ typedef struct fdtd_grid {
                         the same layout the ratios coef_edge / coef_inner used by the
                         adjoint in w = coef * l form */
   const float* pml;  /* NULL (Mur edges, the reference's boundary), or device PML tables of
-                        4 (nx + ny) floats: per column sigma_x at the cell centre, at the left
-                        face, the face decay (1 - sigma dt / 2) / (1 + sigma dt / 2) and the
-                        forcing scale dt / (dx^2 (1 + sigma dt / 2)); then per row the same
-                        for y. The grid then has no Mur edges: it ends in a rigid wall
+                        4 (nx + ny) floats: per column dt sigma_x / 2 at the cell centre and
+                        at the left face, the face decay (1 - sigma dt / 2) / (1 + sigma dt / 2)
+                        and the forcing scale 2 dy^2 / (dx^2 (1 + sigma dt / 2)); then per row
+                        the same for y (forcing scale 2 / (1 + sigma dt / 2)). The grid then has no Mur edges: it ends in a rigid wall
                         behind the layer. */
   int32_t pml_cells; /* layer thickness in cells on every side (with pml) */
 } fdtd_grid;

@@ -101,20 +101,26 @@ __device__ __forceinline__ float inj_add(float un, float inj) { return __fadd_rn
 // factor is exactly 1 or 2 and psi stays 0, so the update is bit for bit the
 // plain leapfrog (leap above).
 
-// One face value psi+ = alpha psi + (sigma_other - sigma_face) beta du.
+// One face value psi+ = alpha psi + (sigma_other - sigma_face) beta du, with the
+// sigmas scaled by dt / 2 and beta by 2 / dt in the tables.
 __device__ __forceinline__ float pml_face(float alpha, float psi, float sig_other, float sig_face, float beta,
                                           float du) {
   return __fmaf_rn(alpha, psi, __fmul_rn(__fmul_rn(__fsub_rn(sig_other, sig_face), beta), du));
 }
 
-// Factors A = q (2 - dt^2 sx sy) and M = (1 - a) q, with a = dt (sx + sy) / 2 and
-// q = 1 / (1 + a), of the cell update u+ = K (Q + div) + A u - M u-, where the
-// coefficient table holds K = q (c dt / dy)^2 and the face fields carry the
-// factor dy^2 of Q (their forcing scale includes it).
-__device__ __forceinline__ void pml_factors(float sxc, float syc, float hdt, float dt2, float& A, float& M) {
-  const float a = __fmul_rn(hdt, __fadd_rn(sxc, syc));
-  const float q = __frcp_rn(__fadd_rn(1.0f, a));
-  A = __fmul_rn(q, __fsub_rn(2.0f, __fmul_rn(dt2, __fmul_rn(sxc, syc))));
+// Factors A = q (2 - dt^2 sx sy) = q (2 - 4 hx hy) and M = (1 - a) q, with
+// a = hx + hy and q = 1 / (1 + a), of the cell update u+ = K (Q + div) + A u - M u-;
+// the tables hold hx = dt sigma_x / 2 and hy = dt sigma_y / 2 at the cell centre,
+// the coefficient table K = q (c dt / dy)^2 (from float64), and the face fields carry
+// the factor dy^2 of Q (their forcing scale includes it). q takes the hardware's
+// approximate reciprocal (the damping factors need no correctly rounded one), and is
+// exactly 1 where a = 0, so that there A = 2 and M = 1 exactly.
+__device__ __forceinline__ void pml_factors(float hx, float hy, float& A, float& M) {
+  const float a = __fadd_rn(hx, hy);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(__fadd_rn(1.0f, a)));
+  const float q = (a == 0.0f) ? 1.0f : r;
+  A = __fmul_rn(q, __fmaf_rn(-4.0f, __fmul_rn(hx, hy), 2.0f));
   M = __fmul_rn(__fsub_rn(1.0f, a), q);
 }
 
@@ -238,11 +244,10 @@ struct TbParams {
   const float* residual;
   double* grad;
   double scale;          // adjoint: dt^2 / dy^2 (the stream holds Q = dy^2 lap), applied per pass
-  // PML (pml != nullptr): tables, update constants dt / 2 and dt^2, the face
-  // fields psi_x / psi_y in and out (nshots, ny, pitch), and the per-CTA capacity
-  // of thread slots holding a thread's face fields in shared memory
+  // PML (pml != nullptr): tables, the face fields psi_x / psi_y in and out
+  // (nshots, ny, pitch), and the per-CTA capacity of thread slots holding a
+  // thread's face fields in shared memory
   const float* pml;
-  float hdt, dt2;
   const float* in_psx;
   const float* in_psy;
   float* out_psx;

@@ -79,7 +79,7 @@ cudaError_t density_chain_launch(int ny, int nx, int pitch, const double* m, con
                                  const double* gk, const double* gbx, const double* gby, const uint8_t* mask,
                                  double* g_m, double* g_rho, cudaStream_t st);
 // One step of a PML grid (fdtd_step_pml): tables, dt / 2, dt^2 and the face fields.
-cudaError_t step_pml_launch(const StepArgs& a, const float* pml, float hdt, float dt2, const float* psx,
+cudaError_t step_pml_launch(const StepArgs& a, const float* pml, const float* psx,
                             const float* psy, float* psx_next, float* psy_next, cudaStream_t st);
 // The PML tables of a padded medium, and coef scaled by q = 1 / (1 + a).
 cudaError_t prepare_pml_launch(const double* c, int ny, int nx, int pitch, double dt, double dx, double dy,

@@ -142,7 +142,7 @@ __global__ void step_kernel(const StepArgs a) {
 // same arithmetic the neighbour does for its own faces), so every value equals
 // the fused kernel's. Beyond the grid u and psi are zero (the rigid wall behind
 // the layer).
-__global__ void step_pml_kernel(const StepArgs a, const float* __restrict__ pml, float hdt, float dt2,
+__global__ void step_pml_kernel(const StepArgs a, const float* __restrict__ pml,
                                 const float* __restrict__ psx, const float* __restrict__ psy, float* psxn,
                                 float* psyn) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,7 +171,7 @@ __global__ void step_pml_kernel(const StepArgs a, const float* __restrict__ pml,
   const float pyb = pml_face(ayf[y], py[i], sxc[x], syf[y], byf[y], __fsub_rn(uc, ud));
   const float pyt = (y + 1 < ny) ? pml_face(ayf[y + 1], py[i + P], sxc[x], syf[y + 1], byf[y + 1], __fsub_rn(uu, uc)) : 0.f;
   float A, M;
-  pml_factors(sxc[x], syc[y], hdt, dt2, A, M);
+  pml_factors(sxc[x], syc[y], A, M);
   float un = pml_leap(uc, a.u_old[s * plane + i], a.coef[i], A, M, lap, pml_div(pxl, pxr, pyb, pyt));
   if (a.src_per_shot > 0) {
     float acc = 0.f;
@@ -228,17 +228,18 @@ __global__ void pml_prepare_kernel(const double* c, int ny, int nx, int pitch, d
   float* row = pml + PML_TABLES * nx;
   for (int i = threadIdx.x; i < nx; i += blockDim.x) {
     const double sc = pml_sigma(i, nx, cells, smx), sf = pml_sigma(i - 0.5, nx, cells, smx);
-    col[i] = (float)sc;
-    col[nx + i] = (float)sf;
+    // sigmas times dt / 2, the forcing scale times 2 / dt (and dy^2, the units of Q)
+    col[i] = (float)(0.5 * dt * sc);
+    col[nx + i] = (float)(0.5 * dt * sf);
     col[2 * nx + i] = (float)((1.0 - 0.5 * dt * sf) / (1.0 + 0.5 * dt * sf));
-    col[3 * nx + i] = (float)(dt * (dy * dy) / (dx * dx * (1.0 + 0.5 * dt * sf)));  // times dy^2 (Q units)
+    col[3 * nx + i] = (float)(2.0 * (dy * dy) / (dx * dx * (1.0 + 0.5 * dt * sf)));
   }
   for (int j = threadIdx.x; j < ny; j += blockDim.x) {
     const double sc = pml_sigma(j, ny, cells, smy), sf = pml_sigma(j - 0.5, ny, cells, smy);
-    row[j] = (float)sc;
-    row[ny + j] = (float)sf;
+    row[j] = (float)(0.5 * dt * sc);
+    row[ny + j] = (float)(0.5 * dt * sf);
     row[2 * ny + j] = (float)((1.0 - 0.5 * dt * sf) / (1.0 + 0.5 * dt * sf));
-    row[3 * ny + j] = (float)(dt / (1.0 + 0.5 * dt * sf));  // dt / dy^2 times dy^2
+    row[3 * ny + j] = (float)(2.0 / (1.0 + 0.5 * dt * sf));  // (dt / dy^2) dy^2 times 2 / dt
   }
   for (long long k = threadIdx.x; k < (long long)ny * nx; k += blockDim.x) {
     const int y = (int)(k / nx), x = (int)(k - (long long)y * nx);
@@ -617,11 +618,11 @@ cudaError_t prepare_medium_launch(const double* c, int ny, int nx, int pitch, do
   return cudaGetLastError();
 }
 
-cudaError_t step_pml_launch(const StepArgs& a, const float* pml, float hdt, float dt2, const float* psx,
+cudaError_t step_pml_launch(const StepArgs& a, const float* pml, const float* psx,
                             const float* psy, float* psx_next, float* psy_next, cudaStream_t st) {
   dim3 block(32, 8);
   dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8, a.n_shots);
-  step_pml_kernel<<<grid, block, 0, st>>>(a, pml, hdt, dt2, psx, psy, psx_next, psy_next);
+  step_pml_kernel<<<grid, block, 0, st>>>(a, pml, psx, psy, psx_next, psy_next);
   return cudaGetLastError();
 }
 

@@ -259,8 +259,6 @@ void fill_params(const fdtd_plan* p, TbParams& q) {
   q.seg_stride = (long long)p->field_elems;
   if (p->pml) {
     q.pml = g.pml;
-    q.hdt = (float)(0.5 * g.dt);
-    q.dt2 = (float)(g.dt * g.dt);
     q.slot_cap = p->slot_cap;
   }
 }
@@ -667,7 +665,7 @@ int32_t fdtd_step_pml(const fdtd_grid* grid, int32_t n_shots, const float* u_old
   a.step = step;
   a.dense = dense;
   a.adjoint = adjoint;
-  cudaError_t e = step_pml_launch(a, grid->pml, (float)(0.5 * grid->dt), (float)(grid->dt * grid->dt), psx, psy,
+  cudaError_t e = step_pml_launch(a, grid->pml, psx, psy,
                                   psx_next, psy_next, (cudaStream_t)stream);
   return e == cudaSuccess ? FDTD_OK : cuda_fail(e, "fdtd_step_pml");
 }

@@ -729,13 +729,13 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
     }
     const float4 co = coefrow<MODE, CS>(p, x, coef4, r);
     float A, M;
-    pml_factors(sxc.x, sy, p.hdt, p.dt2, A, M);
+    pml_factors(sxc.x, sy, A, M);
     P[r][0] = pml_leap(cur.x, P[r][0], co.x, A, M, lA.x, pml_div(pxl.x, pxl.y, pyb.x, pyt.x));
-    pml_factors(sxc.y, sy, p.hdt, p.dt2, A, M);
+    pml_factors(sxc.y, sy, A, M);
     P[r][1] = pml_leap(cur.y, P[r][1], co.y, A, M, lA.y, pml_div(pxl.y, pxl.z, pyb.y, pyt.y));
-    pml_factors(sxc.z, sy, p.hdt, p.dt2, A, M);
+    pml_factors(sxc.z, sy, A, M);
     P[r][2] = pml_leap(cur.z, P[r][2], co.z, A, M, lB.x, pml_div(pxl.z, pxl.w, pyb.z, pyt.z));
-    pml_factors(sxc.w, sy, p.hdt, p.dt2, A, M);
+    pml_factors(sxc.w, sy, A, M);
     P[r][3] = pml_leap(cur.w, P[r][3], co.w, A, M, lB.y, pml_div(pxl.w, pxr3, pyb.w, pyt.w));
     pyb = pyt;
     prv = cur;

@@ -156,15 +156,16 @@ class TorchScalarWave2D:
             self.version += 1
             return
         src = c.detach().cpu().numpy() if isinstance(c, torch.Tensor) else c
-        c64 = torch.tensor(np.asarray(src, dtype=np.float64))
-        if tuple(c64.shape) != self.shape:
-            raise ValueError(f"Sound speed shape {tuple(c64.shape)} does not match {self.shape}.")
-        if not bool(torch.isfinite(c64).all()) or not bool((c64 > 0).all()):
+        arr = np.ascontiguousarray(src, dtype=np.float64)
+        if tuple(arr.shape) != self.shape:
+            raise ValueError(f"Sound speed shape {tuple(arr.shape)} does not match {self.shape}.")
+        if not bool(np.isfinite(arr).all()) or not bool((arr > 0).all()):
             raise ValueError("Sound speed must contain finite positive values.")
-        self._c64.copy_(c64)
-        self._c.copy_(c64)
+        # one host-to-device copy; the float32 and squared copies are made on the device
+        self._c64.copy_(torch.from_numpy(arr))
+        self._c.copy_(self._c64)
         self._c2.copy_(self._c.square())
-        self._c_max = float(c64.max())
+        self._c_max = float(arr.max())
         self.version += 1
 
     def laplacian(self, field):
