@@ -11,8 +11,8 @@
 //   - x-neighbours come from warp shuffles (the warp spans the whole region
 //     width, so no shared memory is needed in x);
 //   - y-neighbours inside a band stay in registers; the first and last row of
-//     every band go through a double-buffered shared-memory exchange, one
-//     __syncthreads per step;
+//     every band go through a double-buffered shared-memory exchange, after
+//     which each neighbouring pair of warps meets on a named barrier (step_sync);
 //   - the region carries a halo of at least nsteps+1 cells at every border that
 //     is not a domain edge, so the cells a tile owns are still exact after the
 //     last step (overlapped temporal blocking); owned cells partition the grid
@@ -20,13 +20,16 @@
 //   - Mur edges and corners (fdtd2d/torch_backend.py:477-490), soft sources
 //     (fdtd2d/torch_backend.py:517), the residual injection
 //     (fdtd2d/torch_backend.py:563-580), the receiver gather
-//     (fdtd2d/torch_backend.py:540-548), the per-step Laplacian of the forward
-//     field (recompute) and the imaging condition
+//     (fdtd2d/torch_backend.py:540-548), the per-step stencil value Q = dy^2 lap
+//     of the forward field (recompute) and the imaging condition
 //     (fdtd2d/torch_backend.py:583-598) are all applied inside the block:
 //     receiver taps and source nodes as per-step shared-memory stages of whole
 //     4-cell rows, Mur coefficients from a per-tile shared-memory table, the
-//     adjoint's gradient tile in tensor memory (tcgen05) and its Laplacian
-//     stream one step ahead through cp.async;
+//     adjoint's gradient tile in tensor memory (tcgen05) and its Q stream one
+//     step ahead through cp.async;
+//   - items are (tile, shot) pairs, costliest tiles first; the forward runs static
+//     runs of consecutive items (reusing the tile's tables) and then takes items
+//     from a per-launch counter, the recompute and adjoint a grid stride;
 //   - each warp runs one of three loop variants per item: no edge work, the
 //     compact edge form (edge rows at fixed band rows, whole-row Mur updates,
 //     corners last) or the general one; the per-step loop of the common cases
@@ -181,8 +184,8 @@ __device__ __forceinline__ float4 coefrow(const TbParams& p, const Ctx& x, const
   return ldg4(x.gcoef + (long long)r * p.pitch);
 }
 
-// Streams lap(u^{n-1}) of this thread's owned rows for adjoint step n into its
-// slots of the shared-memory Laplacian tile, all four columns of a row in one
+// Streams Q(u^{n-1}) = dy^2 lap(u^{n-1}) of this thread's owned rows for adjoint
+// step n into its slots of the shared-memory tile, all four columns of a row in one
 // 16-byte copy (a column the thread does not own reads whatever the segment
 // buffer holds there and is never flushed; xb + 3 < pitch since pitch is a
 // multiple of 4).
@@ -652,7 +655,7 @@ __device__ __forceinline__ float4 pml_face_y(const float4& po, const float4& sxc
 // edges (a PML grid ends in a rigid wall behind the layer: u and psi are zero
 // beyond it). psi_x on a lane's right face is the next lane's left-face value of
 // the same step (a shuffle); psi_y on a band's top face is recomputed from the
-// next band's first row and its published old psi_y, so one barrier per step
+// next band's first row and its published old psi_y, so one step barrier
 // still suffices. Sources, receivers, the recompute's Laplacian and the imaging
 // are as in substep; where sigma = 0 the values are bit for bit the plain ones.
 template <int KY, int MODE, bool CS>
