@@ -96,6 +96,17 @@ __device__ __forceinline__ float4 ldg4(const float* p) {
   return __ldg(reinterpret_cast<const float4*>(p));
 }
 
+// A state row, read once per item: not allocated in L1 (the 128 KB an item loads
+// would otherwise evict the small tables every item reads; measured +0.3 % in the
+// forward and +0.2 % in the gradient).
+__device__ __forceinline__ float4 ldg4_once(const float* p) {
+  float4 v;
+  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
+
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
@@ -837,8 +848,8 @@ __device__ __forceinline__ void load_state(const TbParams& p, const Ctx& x, floa
     const int yy = x.y0 + r;
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
     if (yy >= 0 && yy < p.ny && x.xb < p.pitch) {
-      a = ldg4(p.in_prev + sbase + (long long)yy * p.pitch + x.xb);
-      b = ldg4(p.in_cur + sbase + (long long)yy * p.pitch + x.xb);
+      a = ldg4_once(p.in_prev + sbase + (long long)yy * p.pitch + x.xb);
+      b = ldg4_once(p.in_cur + sbase + (long long)yy * p.pitch + x.xb);
     }
     P[r][0] = a.x; P[r][1] = a.y; P[r][2] = a.z; P[r][3] = a.w;
     C[r][0] = b.x; C[r][1] = b.y; C[r][2] = b.z; C[r][3] = b.w;
@@ -1110,8 +1121,8 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
             const int yy = x.y0 + r;
             float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
             if (yy >= 0 && yy < p.ny && x.xb < p.pitch) {
-              a = ldg4(p.in_psx + sb + (long long)yy * p.pitch + x.xb);
-              b = ldg4(p.in_psy + sb + (long long)yy * p.pitch + x.xb);
+              a = ldg4_once(p.in_psx + sb + (long long)yy * p.pitch + x.xb);
+              b = ldg4_once(p.in_psy + sb + (long long)yy * p.pitch + x.xb);
             }
             x.slot[r] = a;
             x.slot[KY + r] = b;
