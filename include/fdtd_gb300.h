@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FDTD_ABI_VERSION 6
+#define FDTD_ABI_VERSION 7
 
 enum {
   FDTD_OK = 0,
@@ -116,6 +116,13 @@ typedef struct fdtd_tuning {
                                sequence once per set of output pointers and replay it as a
                                CUDA graph; 1: launch every kernel from the host */
   int32_t step_sync;        /* FDTD_SYNC_*: how the warps of a CTA meet after every step */
+  int32_t kept_segments;    /* gradient plans of grids without PML: the last kept_segments
+                               checkpoint segments of the pass have their stencil stream
+                               written by the forward with checkpoints and kept, so the
+                               adjoint recomputes only the segments before them; each takes
+                               ckpt_every * n_shots * ny * pitch * 4 bytes of workspace.
+                               0 = 1 (the recompute's own buffer), negative = none;
+                               fdtd_plan_tuning reports the count in effect (-1: none) */
 } fdtd_tuning;
 
 /* Step synchronisation of the temporally blocked kernel. After every leapfrog step

@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "libfdtd_gb300.so"
-ABI_VERSION = 6
+ABI_VERSION = 7
 
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 
@@ -47,7 +47,7 @@ class Problem(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("rows_per_lane", c_int32), ("warps", c_int32), ("steps_per_launch", c_int32),
                 ("ckpt_every", c_int32), ("ckpt_store", c_int32), ("ctas_per_sm", c_int32),
-                ("eager", c_int32), ("step_sync", c_int32)]
+                ("eager", c_int32), ("step_sync", c_int32), ("kept_segments", c_int32)]
 
     def as_dict(self):
         return {name: int(getattr(self, name)) for name, _ in self._fields_}

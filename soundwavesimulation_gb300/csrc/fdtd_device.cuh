@@ -139,6 +139,13 @@ __device__ __forceinline__ float pml_leap(float c, float p, float K, float A, fl
 constexpr int MODE_FWD = 0;  // forward: sources in, receiver traces out
 constexpr int MODE_REC = 1;  // recompute: sources in, Laplacian of every step out
 constexpr int MODE_ADJ = 2;  // adjoint: residual in, imaging into the gradient
+// forward that also writes the recompute's stencil stream: a gradient plan's forward
+// over the segments whose stream it keeps (their recompute is then skipped)
+constexpr int MODE_FWDQ = 3;
+
+// Modes that record receiver traces / write the stencil stream.
+__host__ __device__ constexpr bool mode_traces(int m) { return m == MODE_FWD || m == MODE_FWDQ; }
+__host__ __device__ constexpr bool mode_stream(int m) { return m == MODE_REC || m == MODE_FWDQ; }
 
 constexpr int RX = 128;       // region width: 32 lanes x 4 columns
 constexpr int TAP_C = 8;      // receivers sharing one tap node

@@ -121,6 +121,9 @@ struct fdtd_plan {
   int nsrc_max = 1, nsrow_max = 0;
   int nrow_max = 0, nrxl_max = 0;
   int adj_coef = 0;
+  // gradient plans: the last `kept` checkpoint segments' stencil streams are written
+  // by the forward (MODE_FWDQ) and kept, so the adjoint recomputes only the others
+  int kept = 0;
   int pair_sync = 0;
   int ckpt_every = 0, nseg = 1;
   size_t field_elems = 0;
@@ -138,7 +141,7 @@ struct fdtd_plan {
   size_t o_sched = 0;  // one item counter per temporally blocked launch of a pass
   int n_sched = 0;
   size_t total = 0;
-  size_t smem[3] = {0, 0, 0};
+  size_t smem[4] = {0, 0, 0, 0};  // per kernel mode (MODE_FWD .. MODE_FWDQ)
   // binding
   char* ws = nullptr;
   size_t ws_bytes = 0;
@@ -898,10 +901,16 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
   // the adjoint keeps its coefficient tile in shared memory when that fits
   p->adj_coef = tb_smem_layout(p->nw, p->ky, MODE_ADJ, p->nrow_max, p->nrxl_max, p->tmax, 1, p->nsrow_max,
                                p->slot_cap).total <= SMEM_LIMIT;
-  for (int m = 0; m < 3; ++m) {
+  p->kept = 0;
+  if (for_gradient && !p->pml) {
+    const int want = t.kept_segments == 0 ? 1 : t.kept_segments;
+    p->kept = want < 0 ? 0 : std::min(want, p->nseg);
+  }
+  p->tun.kept_segments = for_gradient ? (p->kept > 0 ? p->kept : -1) : t.kept_segments;
+  for (int m = 0; m < 4; ++m) {
     p->smem[m] = tb_smem_layout(p->nw, p->ky, m, p->nrow_max, p->nrxl_max, p->tmax, p->adj_coef, p->nsrow_max,
                                 p->slot_cap).total;
-    if (p->smem[m] > SMEM_LIMIT && (m == MODE_FWD || for_gradient)) {
+    if (p->smem[m] > SMEM_LIMIT && (m == MODE_FWD || (for_gradient && (m != MODE_FWDQ || p->kept > 0)))) {
       delete p;
       return fail(FDTD_ERR_UNSUPPORTED, "shared memory need exceeds 227 KB; use fewer steps per launch or warps");
     }
@@ -946,7 +955,9 @@ int32_t fdtd_plan_create(const fdtd_problem* problem, const fdtd_tuning* tuning,
     const size_t nck = (size_t)(p->nseg - 1) * 2;  // checkpoints 1..nseg-1, two fields each
     p->o_ckpt = off; off = align_up(off + nck * p->field_elems * p->ckpt_elem_bytes);
     p->o_scales = off; off = align_up(off + nck * 2 * problem->n_shots * sizeof(float) + 16);
-    p->o_seg = off; off = align_up(off + (size_t)p->ckpt_every * fb);
+    // the recompute's segment buffer; with kept segments, one per kept segment (the
+    // recompute reuses the first once the kept ones are imaged)
+    p->o_seg = off; off = align_up(off + (size_t)std::max(1, p->kept) * p->ckpt_every * fb);
     // the adjoint's imaging sums sum w Q dt^2 / dy^2 (w = coef l), float64 (ny, pitch),
     // divided by coef once per pass into the caller's gradient
     p->o_graw = off; off = align_up(off + (size_t)g.ny * g.pitch * sizeof(double));
@@ -1074,7 +1085,8 @@ int32_t run_graphed(fdtd_plan* p, fdtd_plan::GraphSet& gs, const void* const (&k
     if (!p->capture_stream) e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_fail(e, "capture stream");
     // kernel attributes are set outside the capture
-    for (int m = 0; m < 3; ++m) {
+    for (int m = 0; m < 4; ++m) {
+      if (m == MODE_FWDQ && p->kept == 0) continue;
       e = tb_configure(p->ky, m, p->nw, p->smem[m], p->pml != 0);
       if (e != cudaSuccess) return cuda_fail(e, "kernel attributes");
     }
@@ -1231,13 +1243,15 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
   const float* in_px = p->pml ? fptr(p, p->o_psi[0][0]) : nullptr;
   const float* in_py = p->pml ? fptr(p, p->o_psi[0][1]) : nullptr;
   int psi_set = 0;
+  // segments from kept0 on keep their stencil stream (no checkpoint at their starts)
+  const int kept0 = save_checkpoints ? p->nseg - p->kept : p->nseg;
   for (int n0 = 0; n0 < nt; n0 += T) {
     const int ns = std::min(T, nt - n0), end = n0 + ns;
     const int out_set = (in_set == 0) ? 1 : 0;
     float* out_prev = fptr(p, p->o_state[out_set][0]);
     float* out_cur = fptr(p, p->o_state[out_set][1]);
     int next_set = out_set;
-    const bool ckpt = save_checkpoints && end < nt && end % C == 0;
+    const bool ckpt = save_checkpoints && end < nt && end % C == 0 && end / C < kept0;
     const int j = end / C;
     if (end == nt && u_out) {
       out_prev = u_prev_out;
@@ -1271,7 +1285,14 @@ int32_t forward_enqueue(fdtd_plan* p, float* traces, float* u_prev_out, float* u
       in_px = q.out_psx;
       in_py = q.out_psy;
     }
-    int32_t rc = k.launch_tb(MODE_FWD, q);
+    int mode = MODE_FWD;
+    if (n0 / C >= kept0) {  // a kept segment: its stream into its own buffer
+      const int jq = n0 / C;
+      mode = MODE_FWDQ;
+      q.seg = fptr(p, p->o_seg + (size_t)(jq - kept0) * C * fb);
+      q.seg_base = jq * C;
+    }
+    int32_t rc = k.launch_tb(mode, q);
     if (rc) return rc;
     if (ckpt && p->tun.ckpt_store != FDTD_STORE_F32) {
       const size_t eb = p->field_elems * p->ckpt_elem_bytes;
@@ -1312,82 +1333,89 @@ int32_t adjoint_enqueue(fdtd_plan* p, const float* residual, double* grad_c2, Si
   q.scale = p->prob.grid.dt * p->prob.grid.dt / (p->prob.grid.dy * p->prob.grid.dy);
   q.seg = fptr(p, p->o_seg);
   const int nt = p->prob.n_steps, T = p->tmax, C = p->ckpt_every;
+  const int kept0 = p->nseg - p->kept;  // segments from kept0 on were kept by the forward
   int adj_in = 0;
   const long long per_shot = (long long)p->prob.grid.ny * p->prob.grid.pitch;
   for (int j = p->nseg - 1; j >= 0; --j) {
     const int a = j * C, b = std::min(a + C, nt);
-    const float* in_prev;
-    const float* in_cur;
-    int in_set;
-    // the forward's PML face fields at the segment start
-    const float* in_px = nullptr;
-    const float* in_py = nullptr;
-    int psi_set = 0;
-    if (p->pml) {
-      if (j == 0) {
-        int32_t rc = k.memset(p->ws + p->o_psi[0][0], fb);
-        if (!rc) rc = k.memset(p->ws + p->o_psi[0][1], fb);
-        if (rc) return rc;
-        in_px = fptr(p, p->o_psi[0][0]);
-        in_py = fptr(p, p->o_psi[0][1]);
-      } else {
-        in_px = fptr(p, p->o_ckpsi + (size_t)(j - 1) * 2 * fb);
-        in_py = fptr(p, p->o_ckpsi + ((size_t)(j - 1) * 2 + 1) * fb);
-        psi_set = -1;
-      }
-    }
-    if (j == 0) {
-      int32_t rc = k.memset(p->ws + p->o_state[0][0], fb);
-      if (!rc) rc = k.memset(p->ws + p->o_state[0][1], fb);
-      if (rc) return rc;
-      in_prev = fptr(p, p->o_state[0][0]);
-      in_cur = fptr(p, p->o_state[0][1]);
-      in_set = 0;
-    } else if (p->tun.ckpt_store == FDTD_STORE_F32) {
-      const size_t base = p->o_ckpt + (size_t)(j - 1) * 2 * fb;
-      in_prev = fptr(p, base);
-      in_cur = fptr(p, base + fb);
-      in_set = -1;
+    if (j >= kept0) {  // a kept segment: the forward wrote its stream
+      q.seg = fptr(p, p->o_seg + (size_t)(j - kept0) * C * fb);
+      q.seg_base = a;
     } else {
-      const size_t eb = p->field_elems * p->ckpt_elem_bytes;
-      // u first (slot 1), then u_old = u - (u - u_old) (slot 0)
-      for (int f = 1; f >= 0; --f) {
-        const char* src = p->ws + p->o_ckpt + ((size_t)(j - 1) * 2 + f) * eb;
-        const float* sc = fptr(p, p->o_scales) + ((size_t)(j - 1) * 2 + f) * 2 * p->prob.n_shots;
-        const int32_t rc = k.dequant(src, sc, f == 0 ? fptr(p, p->o_state[0][1]) : nullptr,
-                                     fptr(p, p->o_state[0][f]), p->prob.n_shots, per_shot, p->tun.ckpt_store);
-        if (rc) return rc;
-      }
-      in_prev = fptr(p, p->o_state[0][0]);
-      in_cur = fptr(p, p->o_state[0][1]);
-      in_set = 0;
-    }
-    // recompute the segment, keeping lap(u^{n-1}) of every step n in [a, b)
-    q.seg_base = a;
-    for (int n0 = a; n0 < b; n0 += T) {
-      const int ns = std::min(T, b - n0);
-      const int out_set = (in_set == 0) ? 1 : 0;
-      q.in_prev = in_prev;
-      q.in_cur = in_cur;
-      q.out_prev = fptr(p, p->o_state[out_set][0]);
-      q.out_cur = fptr(p, p->o_state[out_set][1]);
-      q.n0 = n0;
-      q.nsteps = ns;
+      q.seg = fptr(p, p->o_seg);
+      const float* in_prev;
+      const float* in_cur;
+      int in_set;
+      // the forward's PML face fields at the segment start
+      const float* in_px = nullptr;
+      const float* in_py = nullptr;
+      int psi_set = 0;
       if (p->pml) {
-        const int ps_out = (psi_set == 0) ? 1 : 0;
-        q.in_psx = in_px;
-        q.in_psy = in_py;
-        q.out_psx = fptr(p, p->o_psi[ps_out][0]);
-        q.out_psy = fptr(p, p->o_psi[ps_out][1]);
-        in_px = q.out_psx;
-        in_py = q.out_psy;
-        psi_set = ps_out;
+        if (j == 0) {
+          int32_t rc = k.memset(p->ws + p->o_psi[0][0], fb);
+          if (!rc) rc = k.memset(p->ws + p->o_psi[0][1], fb);
+          if (rc) return rc;
+          in_px = fptr(p, p->o_psi[0][0]);
+          in_py = fptr(p, p->o_psi[0][1]);
+        } else {
+          in_px = fptr(p, p->o_ckpsi + (size_t)(j - 1) * 2 * fb);
+          in_py = fptr(p, p->o_ckpsi + ((size_t)(j - 1) * 2 + 1) * fb);
+          psi_set = -1;
+        }
       }
-      int32_t rc = k.launch_tb(MODE_REC, q);
-      if (rc) return rc;
-      in_prev = q.out_prev;
-      in_cur = q.out_cur;
-      in_set = out_set;
+      if (j == 0) {
+        int32_t rc = k.memset(p->ws + p->o_state[0][0], fb);
+        if (!rc) rc = k.memset(p->ws + p->o_state[0][1], fb);
+        if (rc) return rc;
+        in_prev = fptr(p, p->o_state[0][0]);
+        in_cur = fptr(p, p->o_state[0][1]);
+        in_set = 0;
+      } else if (p->tun.ckpt_store == FDTD_STORE_F32) {
+        const size_t base = p->o_ckpt + (size_t)(j - 1) * 2 * fb;
+        in_prev = fptr(p, base);
+        in_cur = fptr(p, base + fb);
+        in_set = -1;
+      } else {
+        const size_t eb = p->field_elems * p->ckpt_elem_bytes;
+        // u first (slot 1), then u_old = u - (u - u_old) (slot 0)
+        for (int f = 1; f >= 0; --f) {
+          const char* src = p->ws + p->o_ckpt + ((size_t)(j - 1) * 2 + f) * eb;
+          const float* sc = fptr(p, p->o_scales) + ((size_t)(j - 1) * 2 + f) * 2 * p->prob.n_shots;
+          const int32_t rc = k.dequant(src, sc, f == 0 ? fptr(p, p->o_state[0][1]) : nullptr,
+                                       fptr(p, p->o_state[0][f]), p->prob.n_shots, per_shot, p->tun.ckpt_store);
+          if (rc) return rc;
+        }
+        in_prev = fptr(p, p->o_state[0][0]);
+        in_cur = fptr(p, p->o_state[0][1]);
+        in_set = 0;
+      }
+      // recompute the segment, keeping lap(u^{n-1}) of every step n in [a, b)
+      q.seg_base = a;
+      for (int n0 = a; n0 < b; n0 += T) {
+        const int ns = std::min(T, b - n0);
+        const int out_set = (in_set == 0) ? 1 : 0;
+        q.in_prev = in_prev;
+        q.in_cur = in_cur;
+        q.out_prev = fptr(p, p->o_state[out_set][0]);
+        q.out_cur = fptr(p, p->o_state[out_set][1]);
+        q.n0 = n0;
+        q.nsteps = ns;
+        if (p->pml) {
+          const int ps_out = (psi_set == 0) ? 1 : 0;
+          q.in_psx = in_px;
+          q.in_psy = in_py;
+          q.out_psx = fptr(p, p->o_psi[ps_out][0]);
+          q.out_psy = fptr(p, p->o_psi[ps_out][1]);
+          in_px = q.out_psx;
+          in_py = q.out_psy;
+          psi_set = ps_out;
+        }
+        int32_t rc = k.launch_tb(MODE_REC, q);
+        if (rc) return rc;
+        in_prev = q.out_prev;
+        in_cur = q.out_cur;
+        in_set = out_set;
+      }
     }
     // reverse-time adjoint over the segment
     for (int ntop = b - 1; ntop >= a; ntop -= T) {
@@ -1474,7 +1502,7 @@ int32_t group_run(fdtd_plan* const* plans, int n, void* workspace, size_t bytes,
       left = left || idx[i] < ops[i].size();
     }
     if (!left) break;
-    for (int m = 0; m < 3; ++m) {
+    for (int m = 0; m < 4; ++m) {
       GroupAction a;
       a.mode = m;
       for (int i = 0; i < n; ++i)

@@ -538,10 +538,10 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   float4 cur = opval(C[0]);
   // Column 0 and column nx-1 are always overwritten by the Mur update, so only
   // the recompute, which stores lap(u) itself, needs the zero outside the domain.
-  const bool lzero = EK != EK_NONE && MODE == MODE_REC && x.lane == 0 && x.rx0 == 0;
-  const bool rzero = EK != EK_NONE && MODE == MODE_REC && x.lane == 31 && (x.rx0 + RX >= p.nx);
+  const bool lzero = EK != EK_NONE && mode_stream(MODE) && x.lane == 0 && x.rx0 == 0;
+  const bool rzero = EK != EK_NONE && mode_stream(MODE) && x.lane == 31 && (x.rx0 + RX >= p.nx);
   float* segrow = nullptr;
-  if (MODE == MODE_REC) {
+  if (mode_stream(MODE)) {
     segrow = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
              ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
   }
@@ -567,7 +567,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
       const float4 co = coefrow<MODE, CS>(p, x, coef4, r);
       const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), Q2, nA);
       const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), Q2, nB);
-      if (MODE == MODE_REC) {
+      if (mode_stream(MODE)) {
         // Q = dy^2 lap (the adjoint's flush scale carries the 1 / dy^2): each
         // owned row in one predicated 16-byte store
         if ((x.rfull >> r) & 1u) *reinterpret_cast<float4*>(segrow) = make_float4(lA.x, lA.y, lB.x, lB.y);
@@ -626,7 +626,7 @@ __device__ __forceinline__ void substep(float (&P)[KY][4], float (&C)[KY][4],
   if (EK == EK_ALL) boundary<KY, MODE == MODE_ADJ>(P, C, p, x);
 
   // ---- receiver taps (forward) / imaging (adjoint)
-  if (MODE == MODE_FWD && x.mask) {
+  if (mode_traces(MODE) && x.mask) {
     // stage every band row that holds a tap node, all four cells of it
     float4* rec = reinterpret_cast<float4*>(x.s_tap) + k * p.nrow_max + x.base;
     int slot = 0;
@@ -701,7 +701,7 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
   float4 pyb = pml_face_y(slot ? slot[KY] : zero4, sxc, syf[r0], ayf[r0], byf[r0], cur, prv);
   const float4 pyb0 = pyb;
   float* segrow = nullptr;
-  if (MODE == MODE_REC) {
+  if (mode_stream(MODE)) {
     segrow = p.seg + (long long)(n - p.seg_base) * p.seg_stride +
              ((long long)x.s * p.ny + x.y0) * p.pitch + x.xb;
   }
@@ -736,7 +736,7 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
     const float2 nB = __ffma2_rn(lrB, R2, udB);
     const float2 lA = __ffma2_rn(make_float2(cur.x, cur.y), Q2, nA);
     const float2 lB = __ffma2_rn(make_float2(cur.z, cur.w), Q2, nB);
-    if (MODE == MODE_REC) {
+    if (mode_stream(MODE)) {
       // Q = dy^2 lap, as substep stores it
       if ((x.rfull >> r) & 1u) *reinterpret_cast<float4*>(segrow) = make_float4(lA.x, lA.y, lB.x, lB.y);
       segrow += p.pitch;
@@ -788,7 +788,7 @@ __device__ __forceinline__ void substep_pml(float (&P)[KY][4], float (&C)[KY][4]
       }
     }
   }
-  if (MODE == MODE_FWD && x.mask) {
+  if (mode_traces(MODE) && x.mask) {
     float4* rec = reinterpret_cast<float4*>(x.s_tap) + k * p.nrow_max + x.base;
     int sl = 0;
 #pragma unroll
@@ -1230,7 +1230,7 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
         }
       }
     }
-    if (MODE == MODE_FWD) {
+    if (mode_traces(MODE)) {
       // receiver traces of the owned receivers, nsteps contiguous samples each
       for (int i = x.tid; i < t.nrec * p.nsteps; i += nthr) {
         const int j = i / p.nsteps, k = i - j * p.nsteps;

@@ -196,6 +196,11 @@ BF16_CHECKPOINT_WARNING = (
     "power-of-two scale per slot and shot) stay near 3e-4")
 
 
+# Share of the free device memory a gradient plan spends on kept stencil streams
+# (each kept checkpoint segment saves its recompute in every adjoint pass).
+KEPT_MEMORY_FRACTION = 0.5
+
+
 class FusedPlan(ProblemTables):
     """One bound plan of the temporally blocked engine over a ProblemTables acquisition."""
 
@@ -208,10 +213,13 @@ class FusedPlan(ProblemTables):
         self.for_gradient = bool(for_gradient)
         self._problem_struct = self.problem()
         t = _lib.Tuning(**{k: int(v) for k, v in (tuning or {}).items()})
-        handle = ctypes.c_void_p()
-        _lib.check(self.lib.fdtd_plan_create(ctypes.byref(self._problem_struct), ctypes.byref(t),
-                                             int(self.for_gradient), ctypes.byref(handle)), "plan")
-        self._plan = handle
+        self._plan = self._create(t)
+        if self.for_gradient and "kept_segments" not in (tuning or {}):
+            kept = self._kept_for_memory(medium)
+            if kept > 1:
+                self.close()
+                t.kept_segments = kept
+                self._plan = self._create(t)
         nbytes = ctypes.c_size_t()
         _lib.check(self.lib.fdtd_plan_workspace_bytes(self._plan, ctypes.byref(nbytes)))
         self.workspace_bytes = int(nbytes.value)
@@ -221,6 +229,29 @@ class FusedPlan(ProblemTables):
         resolved = _lib.Tuning()
         _lib.check(self.lib.fdtd_plan_tuning(self._plan, ctypes.byref(resolved)))
         self.tuning = resolved.as_dict()
+
+    def _create(self, t):
+        handle = ctypes.c_void_p()
+        _lib.check(self.lib.fdtd_plan_create(ctypes.byref(self._problem_struct), ctypes.byref(t),
+                                             int(self.for_gradient), ctypes.byref(handle)), "plan")
+        return handle
+
+    def _kept_for_memory(self, medium) -> int:
+        """Checkpoint segments whose stencil stream the forward keeps: as many as
+        KEPT_MEMORY_FRACTION of the free device memory holds beside the plan's own
+        workspace, at least 1 (grids with PML keep none)."""
+        resolved = _lib.Tuning()
+        _lib.check(self.lib.fdtd_plan_tuning(self._plan, ctypes.byref(resolved)))
+        if resolved.kept_segments < 1:
+            return 0
+        nbytes = ctypes.c_size_t()
+        _lib.check(self.lib.fdtd_plan_workspace_bytes(self._plan, ctypes.byref(nbytes)))
+        every = int(resolved.ckpt_every)
+        n_seg = -(-self.n_steps // every)
+        seg_bytes = every * self.n_shots * medium.ny * medium.pitch * 4
+        free, _ = torch.cuda.mem_get_info(medium.device)
+        extra = int(max(0.0, KEPT_MEMORY_FRACTION * free - int(nbytes.value)) // seg_bytes)
+        return min(n_seg, 1 + extra)
 
     def set_waveforms(self, waveforms: torch.Tensor):
         if tuple(waveforms.shape) != tuple(self.waveforms.shape):

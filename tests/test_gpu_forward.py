@@ -329,11 +329,13 @@ def test_graph_kept_across_in_place_medium_updates(tb):
     assert rel(g.cpu().numpy(), g2.cpu().numpy()) < 1e-12
 
 
-@pytest.mark.parametrize("shape", [{"rows_per_lane": 8, "warps": 16}, {"rows_per_lane": 4, "warps": 32}])
+@pytest.mark.parametrize("shape", [{"rows_per_lane": 8, "warps": 16}, {"rows_per_lane": 4, "warps": 32},
+                                   {"rows_per_lane": 8, "warps": 16, "kept_segments": 1}])
 def test_plan_group_matches_separate_plans(tb, shape):
     """Three grids of different sizes, step counts and temporal-block depths in shared
     launches: traces equal each plan run alone (bitwise), gradients to float64
-    summation order."""
+    summation order; with every segment's stencil stream kept by the forward (the
+    default at these sizes) and with one kept segment (the rest recomputed)."""
     from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan, PlanGroup, residual_misfit
     cases = [(96, 90, 3, 47, 6), (150, 133, 2, 61, 9), (70, 201, 4, 33, 5)]
     plans, alone = [], []

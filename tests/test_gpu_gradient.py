@@ -113,16 +113,13 @@ def test_checkpoint_spacing_and_16bit_storage(mods, golden):
     assert float(np.sum(g * g_ref) / (np.linalg.norm(g) * np.linalg.norm(g_ref))) > 0.999
 
 
-@pytest.mark.parametrize("tuning", [{"steps_per_launch": 10},
-                                    {"steps_per_launch": 9, "rows_per_lane": 4, "warps": 32},
-                                    {"steps_per_launch": 7, "rows_per_lane": 8, "warps": 12}])
-def test_fused_gradient_equals_plain_form(mods, tuning):
-    """Checkpointed fused gradient vs the plain per-shot full-history gradient, per launch shape."""
-    from soundwavesimulation_gb300.engine import DeviceMedium, FusedPlan, ProblemTables, gradient_plain
-    from soundwavesimulation_gb300.engine import residual_misfit
+def _ellipse_gradient_case(nt=300):
+    """150^2 ellipse medium, 3 shots of a 40-element ring, a start model with the
+    inclusions halved: (true medium, start medium, ring, tx, sources, waveforms, nt)."""
+    from soundwavesimulation_gb300.engine import DeviceMedium
     from soundwavesimulation_gb300.phantoms import random_ellipses
     from soundwavesimulation_gb300 import RingArray, axis_centers, stable_dt, ricker
-    n, dx, nt = 150, 0.35e-3, 300
+    n, dx = 150, 0.35e-3
     c, _ = random_ellipses(n, dx, 5, seed=3)
     dt = stable_dt(float(c.max()), dx, dx, cfl=0.3)
     x = axis_centers(n, dx)
@@ -132,8 +129,23 @@ def test_fused_gradient_equals_plain_form(mods, tuning):
     src = (rows, cols, np.ones(rows.shape), np.zeros(rows.shape, dtype=np.int64))
     waves = torch.as_tensor(ricker(3e5, dt, nt)[None], dtype=torch.float32, device="cuda")
     true = DeviceMedium(c, dx, dx, dt, "cuda")
-    observed = FusedPlan(true, ring.receiver_taps(), src, waves, nt).forward().clone()
     start = DeviceMedium(np.where(c > 1500.0, 0.5 * (c + 1500.0), c), dx, dx, dt, "cuda")
+    return true, start, ring, tx, src, waves, nt
+
+
+@pytest.mark.parametrize("tuning", [{"steps_per_launch": 10},
+                                    {"steps_per_launch": 10, "kept_segments": -1},
+                                    {"steps_per_launch": 9, "rows_per_lane": 4, "warps": 32},
+                                    {"steps_per_launch": 7, "rows_per_lane": 8, "warps": 12}])
+def test_fused_gradient_equals_plain_form(mods, tuning):
+    """Checkpointed fused gradient vs the plain per-shot full-history gradient, per launch
+    shape; with every segment's stencil stream kept by the forward (the default at this
+    size) and with every segment recomputed (kept_segments -1)."""
+    from soundwavesimulation_gb300.engine import FusedPlan, ProblemTables, gradient_plain
+    from soundwavesimulation_gb300.engine import residual_misfit
+    true, start, ring, tx, src, waves, nt = _ellipse_gradient_case()
+    n = start.ny
+    observed = FusedPlan(true, ring.receiver_taps(), src, waves, nt).forward().clone()
     plan = FusedPlan(start, ring.receiver_taps(), src, waves, nt, for_gradient=True, tuning=tuning)
     traces = plan.forward(save_checkpoints=True)
     res, J = residual_misfit(traces, observed, tx)
@@ -142,6 +154,41 @@ def test_fused_gradient_equals_plain_form(mods, tuning):
     Jp, gp = gradient_plain(ProblemTables(start, ring.receiver_taps(), src, waves, nt), observed, tx)
     assert float(J) == pytest.approx(float(Jp), rel=1e-6)
     assert rel(g.cpu(), gp.cpu()) < 1e-6
+
+
+@pytest.mark.parametrize("store", [0, 1])
+def test_kept_segments_leave_traces_and_gradient_unchanged(mods, store):
+    """The forward keeps the stencil stream of the last kept_segments checkpoint
+    segments (their recompute is skipped): traces are bit for bit those of the plain
+    forward, and the gradient equals the all-recompute gradient to float64 summation
+    order with float32 checkpoints (16-bit checkpoints: the kept segments image the
+    exact stream, the recomputed ones the stream from rounded checkpoints)."""
+    from soundwavesimulation_gb300.engine import FusedPlan, residual_misfit
+    true, start, ring, tx, src, waves, nt = _ellipse_gradient_case(nt=290)
+    observed = FusedPlan(true, ring.receiver_taps(), src, waves, nt).forward().clone()
+    base = {"steps_per_launch": 10, "ckpt_every": 30, "ckpt_store": store}  # 10 segments, the last short
+    ref_plan = FusedPlan(start, ring.receiver_taps(), src, waves, nt, for_gradient=True,
+                         tuning={**base, "kept_segments": -1})
+    assert ref_plan.tuning["kept_segments"] == -1
+    ref_tr = ref_plan.forward(save_checkpoints=True).clone()
+    res, _ = residual_misfit(ref_tr, observed, tx)
+    g_ref = torch.zeros((start.ny, start.pitch), dtype=torch.float64, device="cuda")
+    ref_plan.adjoint(res, g_ref)
+    for kept in (1, 3, 10, 25):
+        plan = FusedPlan(start, ring.receiver_taps(), src, waves, nt, for_gradient=True,
+                         tuning={**base, "kept_segments": kept})
+        assert plan.tuning["kept_segments"] == min(kept, 10)
+        tr = plan.forward(save_checkpoints=True)
+        assert torch.equal(tr, ref_tr)
+        res_k, _ = residual_misfit(tr, observed, tx)
+        g = torch.zeros_like(g_ref)
+        plan.adjoint(res_k, g)
+        assert rel(g.cpu(), g_ref.cpu()) < (1e-12 if store == 0 else 2e-3), kept
+        # a second pass through the same plan (graph replay) gives the same gradient
+        g2 = torch.zeros_like(g_ref)
+        plan.forward(save_checkpoints=True)
+        plan.adjoint(res_k, g2)
+        assert rel(g2.cpu(), g.cpu()) < 1e-12
 
 
 def _fd_problem(mods, n_shots):
