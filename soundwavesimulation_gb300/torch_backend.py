@@ -626,22 +626,34 @@ class TorchFDTD2DBatch:
 
 
 def simulate_shots_batch(solver: TorchFDTD2D, sampler: TorchRingSampler, pulse, source_rows, source_cols,
-                         n_steps: int, batched: TorchFDTD2DBatch | None = None, source_values=None):
+                         n_steps: int, batched: TorchFDTD2DBatch | None = None, source_values=None, out=None):
     """All shots of a batch through the fused engine (fdtd2d/torch_backend.py:736-770).
 
     Returns traces ``(shots, receivers, n_steps)`` and the final field batch.
+    ``out`` (optional, not in the reference's signature) receives the traces: a
+    contiguous float32 tensor of that shape on the solver's device, or in pinned
+    host memory, which the kernels then write directly over the host link (no copy
+    after the run; synchronise the device before reading it, as after a
+    non-blocking copy).
     """
     if batched is None:
         batched = TorchFDTD2DBatch(solver, len(source_rows))
     elif batched.n_shots != len(source_rows):
         raise ValueError("Batched solver size does not match the source batch.")
+    if out is not None:
+        shape = (len(source_rows), sampler.n_elements, int(n_steps))
+        on_device = out.device == solver.medium.device
+        if out.dtype != torch.float32 or not out.is_contiguous() or tuple(out.shape) != shape:
+            raise ValueError(f"out must be a contiguous float32 tensor of shape {shape}.")
+        if not on_device and not (out.device.type == "cpu" and out.is_pinned()):
+            raise ValueError("out must live on the solver's device or in pinned host memory.")
     batched.set_sources(source_rows, source_cols)
     values = _source_values(solver, pulse, n_steps, source_values)
     solver._sync_medium()
     plan = _plan_for(batched, solver, sampler, batched._rows_h, batched._cols_h, n_steps, values[None])
     r = batched._rot
     r.io, r.ic, r.inx = 0, 1, 2
-    traces = plan.forward(u_prev_out=r.buf[0], u_out=r.buf[1])
+    traces = plan.forward(traces=out, u_prev_out=r.buf[0], u_out=r.buf[1])
     return traces, batched.u
 
 

@@ -92,6 +92,31 @@ def test_fused_ring41_matches_reference(tb, golden):
     assert rel(u.cpu(), d["batched_u"]) < FIELD_TOL
 
 
+def test_traces_written_into_pinned_host_out(tb, golden):
+    """simulate_shots_batch(out=...): a pinned host tensor is written by the kernels
+    directly (bit for bit the device result, no copy); a device tensor likewise;
+    pageable host memory and wrong shapes are refused before any launch."""
+    d, solver, array, sampler = ring41_objects(tb, golden)
+    nt = int(d["n_steps"])
+    pulse = torch.as_tensor(d["pulse"])
+    ref, _ = tb.simulate_shots_batch(solver, sampler, pulse, array.rows, array.cols, nt)
+    ref = ref.clone()
+    host = torch.full((6, 6, nt), float("nan"), dtype=torch.float32, pin_memory=True)
+    got, _ = tb.simulate_shots_batch(solver, sampler, pulse, array.rows, array.cols, nt, out=host)
+    torch.cuda.synchronize()
+    assert got.data_ptr() == host.data_ptr()
+    assert torch.equal(host, ref.cpu())
+    dev = torch.empty_like(ref)
+    tb.simulate_shots_batch(solver, sampler, pulse, array.rows, array.cols, nt, out=dev)
+    assert torch.equal(dev, ref)
+    with pytest.raises(ValueError):
+        tb.simulate_shots_batch(solver, sampler, pulse, array.rows, array.cols, nt,
+                                out=torch.empty((6, 6, nt), dtype=torch.float32))
+    with pytest.raises(ValueError):
+        tb.simulate_shots_batch(solver, sampler, pulse, array.rows, array.cols, nt,
+                                out=torch.empty((6, 5, nt), dtype=torch.float32, pin_memory=True))
+
+
 def test_single_shot_matches_reference(tb, golden):
     d, solver, array, sampler = ring41_objects(tb, golden)
     nt = int(d["n_steps"])
