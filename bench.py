@@ -38,7 +38,7 @@ GRAD_BYTES_PER_CELL = 28.0   # forward 12 + adjoint 12 + one read of the forward
 # capture of that launch, keyed by the digest of the kernel sources it was taken on
 # and the launch shape (rows per lane, warps, steps per launch). A bench run on
 # other sources or another shape reports the figure as null.
-FWD_TRAFFIC = {("292f88e7d78e", 8, 16, 15): 397.730304e6 + 218.976000e6}
+FWD_TRAFFIC = {("0510d886fb66", 8, 16, 15): 398.682880e6 + 219.159296e6}
 KERNEL_SOURCES = ("soundwavesimulation_gb300/csrc/fdtd_tb.cu", "soundwavesimulation_gb300/csrc/fdtd_tb.cuh",
                   "soundwavesimulation_gb300/csrc/fdtd_device.cuh")
 

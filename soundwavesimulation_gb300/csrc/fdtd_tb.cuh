@@ -838,9 +838,9 @@ __device__ __forceinline__ void store_state(const TbParams& p, const Ctx& x,
 }
 
 // The item's two state fields, this thread's band rows (zero outside the domain;
-// padding columns start at zero whatever the buffer holds there). Issued at the
-// start of the item so that their latency overlaps the table setup.
-template <int KY>
+// padding columns: see zero_padding). Issued at the start of the item so that
+// their latency overlaps the table setup.
+template <int KY, bool LATE_PAD>
 __device__ __forceinline__ void load_state(const TbParams& p, const Ctx& x, float (&P)[KY][4], float (&C)[KY][4]) {
   const long long sbase = (long long)x.s * p.ny * p.pitch;
 #pragma unroll
@@ -853,6 +853,25 @@ __device__ __forceinline__ void load_state(const TbParams& p, const Ctx& x, floa
     }
     P[r][0] = a.x; P[r][1] = a.y; P[r][2] = a.z; P[r][3] = a.w;
     C[r][0] = b.x; C[r][1] = b.y; C[r][2] = b.z; C[r][3] = b.w;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      if (!LATE_PAD && x.xb + c >= p.nx) { P[r][c] = 0.f; C[r][c] = 0.f; }
+    }
+  }
+}
+
+// Padding columns (x >= nx) start every item at zero whatever the buffer holds
+// there. With LATE_PAD (every mode but the adjoint) this runs at the end of the item
+// setup, not in load_state: overwriting a register that a load is still filling
+// waits for the load, which would hold the whole setup behind the state's latency
+// (the forward measured 2.3 % faster; the adjoint, at its register limit, spilled
+// more and kept the early form).
+template <int KY>
+__device__ __forceinline__ void zero_padding(const TbParams& p, const Ctx& x, float (&P)[KY][4],
+                                             float (&C)[KY][4]) {
+  if (x.xb + 3 < p.nx) return;
+#pragma unroll
+  for (int r = 0; r < KY; ++r) {
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       if (x.xb + c >= p.nx) { P[r][c] = 0.f; C[r][c] = 0.f; }
@@ -998,7 +1017,8 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
       x.rfull = (x.own_cols && ext == 0xFu) ? x.own_rows : 0u;
     }
     float P[KY][4], C[KY][4];
-    load_state<KY>(p, x, P, C);
+    constexpr bool LATE_PAD = MODE != MODE_ADJ;
+    load_state<KY, LATE_PAD>(p, x, P, C);
     if (next >= 0) prefetch_state<KY>(p, x, next);
 
     // coefficients of the region (zero outside the domain; the padding columns of
@@ -1176,6 +1196,7 @@ __device__ __forceinline__ void run_one(const TbParams& p, Ctx& x, unsigned char
     // row (shot-independent, from the plan), and the band's first and last rows
     // for the first step
     const int2 tmk = __ldg(reinterpret_cast<const int2*>(p.tmask) + (long long)ti * nthr + x.tid);
+    if (LATE_PAD) zero_padding<KY>(p, x, P, C);
     x.s_xch[x.w * 64 + x.lane] = opval(C[0]);
     x.s_xch[x.w * 64 + 32 + x.lane] = opval(C[KY - 1]);
     if (ASYNC_FILL) {  // the coefficient and Mur table copies
