@@ -218,3 +218,40 @@ def test_plain_entry_points_validate_sources_and_receivers(bad):
     prob_ok, keep_ok = _fake_problem()
     # a valid problem passes the checks and fails only on the too-small workspace
     assert lib.fdtd_forward_plain(ctypes.byref(prob_ok), 0x4000, 0x5000, 16, None) == 3
+
+
+def test_kept_segments_resolution_and_workspace():
+    """fdtd_tuning.kept_segments on a gradient plan (host-side planning only, no
+    device work): 0 keeps one segment (the recompute's own buffer), a negative
+    count none (reported as -1), larger counts are capped at the number of
+    checkpoint segments, and every kept segment beyond the first adds one segment
+    buffer (ckpt_every fields) to the workspace."""
+    import ctypes
+    from soundwavesimulation_gb300 import _lib
+    lib = _lib.load()
+    prob, keep = _fake_problem(n=200)
+    prob.n_steps = 300
+    field = 1 * 200 * 200 * 4  # shots x ny x pitch x float32
+    got = {}
+    for kept in (0, -3, 1, 2, 100):
+        t = _lib.Tuning(steps_per_launch=10, ckpt_every=30, kept_segments=kept)
+        h = ctypes.c_void_p()
+        assert lib.fdtd_plan_create(ctypes.byref(prob), ctypes.byref(t), 1, ctypes.byref(h)) == 0
+        r = _lib.Tuning()
+        nb = ctypes.c_size_t()
+        assert lib.fdtd_plan_tuning(h, ctypes.byref(r)) == 0
+        assert lib.fdtd_plan_workspace_bytes(h, ctypes.byref(nb)) == 0
+        lib.fdtd_plan_destroy(h)
+        got[kept] = (r.kept_segments, nb.value)
+    assert [got[k][0] for k in (0, -3, 1, 2, 100)] == [1, -1, 1, 2, 10]
+    assert got[0][1] == got[1][1] == got[-3][1]
+    assert got[2][1] - got[1][1] == 30 * field
+    assert got[100][1] - got[1][1] == 9 * 30 * field
+    # a forward-only plan keeps nothing and reports the count it was given
+    t = _lib.Tuning(steps_per_launch=10, kept_segments=0)
+    h = ctypes.c_void_p()
+    assert lib.fdtd_plan_create(ctypes.byref(prob), ctypes.byref(t), 0, ctypes.byref(h)) == 0
+    r = _lib.Tuning()
+    assert lib.fdtd_plan_tuning(h, ctypes.byref(r)) == 0
+    lib.fdtd_plan_destroy(h)
+    assert r.kept_segments == 0
