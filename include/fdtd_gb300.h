@@ -284,18 +284,20 @@ int32_t fdtd_plan_set_medium(fdtd_plan* plan, const float* coef, const float* mu
                              const float* waveforms);
 
 /* Batched forward of every shot over n_steps with the fused temporally blocked
-   kernel. traces: device (n_shots, n_rx, n_steps). u_prev_out / u_out
-   (nullable, device (n_shots, ny, pitch)) receive the last two fields.
-   save_checkpoints = 1 keeps the checkpoints a later fdtd_adjoint needs.
+   kernel. traces: (n_shots, n_rx, n_steps), device memory or pinned host memory
+   (which the kernels then write directly). u_prev_out / u_out (nullable, device
+   (n_shots, ny, pitch)) receive the last two fields. save_checkpoints = 1 keeps
+   what a later fdtd_adjoint needs: the checkpoints of the segments it will
+   recompute and the stencil stream of the kept segments (kept_segments).
    Replaces simulate_shots_batch (fdtd2d/torch_backend.py:736-770) and
    forward_store_batch (invert_ring.py:422-455). */
 int32_t fdtd_forward(fdtd_plan* plan, float* traces, float* u_prev_out, float* u_out,
                      int32_t save_checkpoints, void* stream);
 
 /* Reverse-time adjoint of the last checkpointed forward: injects `residual`
-   (device (n_shots, n_rx, n_steps)), recomputes each checkpoint segment and
-   adds dt^2 * sum_{shots, n >= 1} adj^n * lap(u^{n-1}) into grad_c2 (device
-   float64 (ny, pitch)).
+   (device (n_shots, n_rx, n_steps)), recomputes each checkpoint segment that the
+   forward did not keep and adds dt^2 * sum_{shots, n >= 1} adj^n * lap(u^{n-1})
+   into grad_c2 (device float64 (ny, pitch)).
    Replaces _adjoint_accumulate_batch (invert_ring.py:683-701) with
    store_every = 1. */
 int32_t fdtd_adjoint(fdtd_plan* plan, const float* residual, double* grad_c2, void* stream);
