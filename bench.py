@@ -288,7 +288,7 @@ def bench_gradient(args, acq, medium, rx, waves, observed, tuning, device, world
     stream = torch.cuda.current_stream()
     ms = timed(plan, args.steps)
     # the plan keeps the stencil stream of its last kept_segments checkpoint segments
-    # (half of the free device memory); freed before the next plans take their share
+    # (60 % of the free device memory); freed before the next plans take their share
     plan_tuning, plan_ws = dict(plan.tuning), plan.workspace_bytes
     del plan
     torch.cuda.empty_cache()

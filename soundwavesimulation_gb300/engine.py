@@ -198,7 +198,7 @@ BF16_CHECKPOINT_WARNING = (
 
 # Share of the free device memory a gradient plan spends on kept stencil streams
 # (each kept checkpoint segment saves its recompute in every adjoint pass).
-KEPT_MEMORY_FRACTION = 0.5
+KEPT_MEMORY_FRACTION = 0.6
 
 
 class FusedPlan(ProblemTables):
