@@ -202,7 +202,13 @@ KEPT_MEMORY_FRACTION = 0.6
 
 
 class FusedPlan(ProblemTables):
-    """One bound plan of the temporally blocked engine over a ProblemTables acquisition."""
+    """One bound plan of the temporally blocked engine over a ProblemTables acquisition.
+
+    ``tuning`` takes the ``fdtd_tuning`` fields by name. A gradient plan whose tuning
+    does not name ``kept_segments`` keeps the stencil stream of as many of its last
+    checkpoint segments as KEPT_MEMORY_FRACTION of the free device memory holds
+    (at least one); ``self.tuning`` reports the count in effect.
+    """
 
     def __init__(self, medium: DeviceMedium, receivers, sources, waveforms: torch.Tensor,
                  n_steps: int, tuning: dict | None = None, for_gradient: bool = False):
